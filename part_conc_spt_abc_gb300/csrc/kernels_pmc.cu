@@ -1,0 +1,839 @@
+/*
+ * kernels_pmc.cu -- the ABC-PMC step on the device.
+ *
+ * The reference runs the population Monte Carlo loop on the host in double
+ * (SimulationT::run, src/gpu/detail/simulation_impl.inl:178-455): per slot it
+ * picks a parent by weight (wrand_idx_ :54-62), perturbs every parameter with
+ * a reflected Gaussian (displace_ :64-79), sorts components by m to avoid
+ * label switching (:276-303), draws Poisson particle counts (:307-317), ships
+ * one proposal per launch and retries the slot until dist <= gamma; at the
+ * end of a generation it reweights (:832-887), updates tau (:733-749) and
+ * lowers gamma.  Here the same steps run as kernels over all pending slots of
+ * all jobs in a round:
+ *
+ *   k_round_plan   shares the round's proposal capacity among the jobs
+ *                  (trials per pending slot k = capacity / pending, clamped)
+ *   k_propose      one thread per proposal: parent pick, perturbation,
+ *                  label sort, per-proposal forward-model arguments, Poisson
+ *                  counts per video (transformed rejection, Hoermann 1993)
+ *   k_items        scan of work items and the item -> proposal map
+ *   k_accept       per job: first accepted trial of every slot, trial
+ *                  accounting, compaction of the pending list
+ *   k_whiten       coordinates of old/new populations in the metric of the
+ *                  perturbation kernel (double -> float, centred)
+ *   k_kernel_sum   pmc-standard importance weights: log-sum-exp over the old
+ *                  population in FP32
+ *   k_finalize     per job: weight normalisation (FP64), commit, tau or
+ *                  weighted covariance + Cholesky (FP64), gamma update
+ *
+ * Every random draw is Philox keyed by (seed, generation, slot, trial), so a
+ * job's result does not depend on the round capacity or on which other jobs
+ * share its rounds.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "pcs_common.h"
+#include "pcs_kernels.h"
+
+namespace pcs {
+
+namespace {
+
+__device__ __forceinline__ double u53_(pcs_u4 r, int half)
+{
+    return half ? pcs_u01_53(r.z, r.w) : pcs_u01_53(r.x, r.y);
+}
+
+/* standard normal pair from 4 words (Box-Muller, double) */
+__device__ __forceinline__ void normal2_(pcs_u4 r, double& n0, double& n1)
+{
+    double u1 = 1.0 - pcs_u01_53(r.x, r.y); /* (0, 1] */
+    double u2 = pcs_u01_53(r.z, r.w);
+    double rad = sqrt(-2.0 * log(u1));
+    double s, c;
+    sincospi(2.0 * u2, &s, &c);
+    n0 = rad * s;
+    n1 = rad * c;
+}
+
+/* displace_ reflection (simulation_impl.inl:72-76), with a bounded loop */
+__device__ double reflect_(double bis, double lo, double hi)
+{
+    for (int it = 0; it < 64 && (bis < lo || bis > hi); ++it) {
+        if (bis < lo) bis += 2.0 * (lo - bis);
+        if (bis > hi) bis -= 2.0 * (bis - hi);
+    }
+    if (bis < lo || bis > hi) {
+        /* far outside: fold with the period of the reflection */
+        double w = hi - lo;
+        double t = fmod(fabs(bis - lo), 2.0 * w);
+        bis = lo + (t <= w ? t : 2.0 * w - t);
+    }
+    return bis;
+}
+
+/* Poisson(lambda): inversion for small means, PTRS transformed rejection
+ * (W. Hoermann, "The transformed rejection method for generating Poisson
+ * random variables", Insurance: Mathematics and Economics 12, 1993). */
+__device__ uint32_t poisson_(double lam, uint32_t video, uint32_t slot, uint32_t gt, uint32_t k0,
+                             uint32_t k1)
+{
+    if (!(lam > 0.0)) return 0u;
+    if (lam < 12.0) {
+        pcs_u4 r = pcs_philox(video, pcs_ctr_tag(PCS_STREAM_POISSON, 0u), slot, gt, k0, k1);
+        double u = pcs_u01_53(r.x, r.y);
+        double p = exp(-lam), F = p;
+        uint32_t k = 0;
+        while (u > F && k < 1000u) {
+            ++k;
+            p *= lam / k;
+            F += p;
+        }
+        return k;
+    }
+    const double slam = sqrt(lam), loglam = log(lam);
+    const double b = 0.931 + 2.53 * slam;
+    const double a = -0.059 + 0.02483 * b;
+    const double invalpha = 1.1239 + 1.1328 / (b - 3.4);
+    const double vr = 0.9277 - 3.6224 / (b - 2.0);
+    for (uint32_t it = 0; it < 256u; ++it) {
+        pcs_u4 r = pcs_philox(video, pcs_ctr_tag(PCS_STREAM_POISSON, 1u + it), slot, gt, k0, k1);
+        double U = pcs_u01_53(r.x, r.y) - 0.5;
+        double V = pcs_u01_53(r.z, r.w);
+        double us = 0.5 - fabs(U);
+        double kf = floor((2.0 * a / us + b) * U + lam + 0.43);
+        if (us >= 0.07 && V <= vr) return (uint32_t)kf;
+        if (kf < 0.0 || (us < 0.013 && V > us)) continue;
+        if (log(V) + log(invalpha) - log(a / (us * us) + b) <= -lam + kf * loglam - lgamma(kf + 1.0))
+            return (uint32_t)kf;
+    }
+    return (uint32_t)floor(lam + 0.5);
+}
+
+/* index of the first cumulative weight >= u (std::lower_bound), clamped */
+__device__ uint32_t pick_(const double* wcum, uint32_t N, double u)
+{
+    uint32_t lo = 0, hi = N;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (wcum[mid] < u)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo < N ? lo : N - 1;
+}
+
+__device__ uint32_t job_of_(const RoundDev* rd, uint32_t q)
+{
+    uint32_t j = 0;
+    for (uint32_t i = 1; i < rd->n_jobs; ++i)
+        if (rd->job_base[i] <= q && rd->job_count[i] > 0) j = i;
+    /* job_base is non-decreasing; pick the last job whose range contains q */
+    for (uint32_t i = 0; i < rd->n_jobs; ++i)
+        if (q >= rd->job_base[i] && q < rd->job_base[i] + rd->job_count[i]) return i;
+    return j;
+}
+
+/* parameter layout: [m | s (lognormal) | log10c | az] */
+struct Layout {
+    uint32_t m, s, c, az, C, Z;
+};
+
+__device__ __forceinline__ Layout layout_(const JobPmcDev& pm)
+{
+    Layout L;
+    L.C = pm.C;
+    L.Z = pm.Z;
+    L.m = 0;
+    L.s = pm.C;
+    L.c = (pm.model == PCS_DEV_MODEL_LOGNORMAL) ? 2 * pm.C : pm.C;
+    L.az = L.c + pm.C;
+    return L;
+}
+
+} // namespace
+
+/* ----------------------------------------------------------------------- */
+__global__ void k_round_plan(PmcArgs a)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    RoundDev* rd = a.round;
+    uint64_t total_pending = 0;
+    for (uint32_t j = 0; j < rd->n_jobs; ++j) {
+        const JobPmcDev& pm = a.pmc[j];
+        if (!pm.done) total_pending += pm.pending_count;
+    }
+    uint32_t k = total_pending ? (uint32_t)(rd->capacity / total_pending) : 1u;
+    if (k < 1u) k = 1u;
+    if (k > rd->max_spec) k = rd->max_spec;
+    uint32_t base = 0;
+    uint64_t hbase = 0;
+    for (uint32_t j = 0; j < rd->n_jobs; ++j) {
+        const JobPmcDev& pm = a.pmc[j];
+        uint32_t kj = (pm.generation == 0u) ? 1u : k; /* prior pass: one simulation per slot */
+        uint64_t want = pm.done ? 0u : (uint64_t)pm.pending_count * kj;
+        uint64_t room = rd->capacity - base;
+        const uint64_t rb = (uint64_t)a.jobs[j].R * a.jobs[j].B;
+        if (rb) {
+            uint64_t hroom = (rd->hist_cap - hbase) / rb;
+            if (hroom < room) room = hroom;
+        }
+        uint64_t cnt = want < room ? want : room;
+        cnt -= cnt % kj; /* whole slots only */
+        rd->job_base[j] = base;
+        rd->job_k[j] = kj;
+        rd->job_count[j] = (uint32_t)cnt;
+        rd->job_hist_base[j] = hbase;
+        base += (uint32_t)cnt;
+        hbase += cnt * rb;
+    }
+    rd->n_props = base;
+    rd->n_items = 0u;
+    rd->queue_head = 0u;
+}
+
+/* ----------------------------------------------------------------------- */
+__global__ void __launch_bounds__(128) k_propose(PmcArgs a)
+{
+    const RoundDev* rd = a.round;
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= rd->n_props) return;
+    const uint32_t j = job_of_(rd, q);
+    JobPmcDev& pm = a.pmc[j];
+    const JobDev& jd = a.jobs[j];
+    const uint32_t k = rd->job_k[j];
+    const uint32_t local = q - rd->job_base[j];
+    const uint32_t pend_idx = local / k, rep = local % k;
+    const uint32_t slot = pm.pending[pend_idx];
+    const uint32_t trial = pm.next_trial[slot] + rep;
+    const uint32_t gen = pm.generation;
+    const uint32_t gt = pcs_ctr_gen_trial(gen, trial);
+    const uint32_t k0 = jd.seed_lo, k1 = jd.seed_hi;
+    const uint32_t P = pm.P, N = pm.N;
+    const Layout L = layout_(pm);
+
+    double th[PCS_MAX_P];
+    if (gen == 0u) {
+        for (uint32_t p = 0; p < P; ++p) th[p] = pm.theta[(uint64_t)slot * P + p];
+    } else {
+        pcs_u4 r = pcs_philox(0u, pcs_ctr_tag(PCS_STREAM_PICK, 0u), slot, gt, k0, k1);
+        const uint32_t parent = pick_(pm.wcum, N, u53_(r, 0));
+        const double* tp = pm.theta + (uint64_t)parent * P;
+        double nrm[PCS_MAX_P];
+        for (uint32_t p = 0; p < P; p += 2) {
+            pcs_u4 rr = pcs_philox(p >> 1, pcs_ctr_tag(PCS_STREAM_PERTURB, 0u), slot, gt, k0, k1);
+            double n0, n1;
+            normal2_(rr, n0, n1);
+            nrm[p] = n0;
+            if (p + 1 < P) nrm[p + 1] = n1;
+        }
+        for (uint32_t p = 0; p < P; ++p) {
+            if (pm.fixed[p]) {
+                th[p] = pm.lo[p];
+                continue;
+            }
+            double delta;
+            if (pm.perturbation == 1u) {
+                delta = 0.0;
+                for (uint32_t i = 0; i <= p; ++i)
+                    if (!pm.fixed[i]) delta += pm.factor[p * P + i] * nrm[i];
+            } else {
+                delta = pm.factor[p * P + p] * nrm[p];
+            }
+            th[p] = reflect_(tp[p] + delta, pm.lo[p], pm.hi[p]);
+        }
+        /* sort components by the first parameter group (label switching) */
+        for (uint32_t i = 1; i < L.C; ++i) {
+            for (uint32_t x = i; x > 0 && th[L.m + x] < th[L.m + x - 1]; --x) {
+                double t;
+                t = th[L.m + x]; th[L.m + x] = th[L.m + x - 1]; th[L.m + x - 1] = t;
+                t = th[L.c + x]; th[L.c + x] = th[L.c + x - 1]; th[L.c + x - 1] = t;
+                if (pm.model == PCS_DEV_MODEL_LOGNORMAL) {
+                    t = th[L.s + x]; th[L.s + x] = th[L.s + x - 1]; th[L.s + x - 1] = t;
+                }
+                if (L.Z > 1u) {
+                    t = th[L.az + x]; th[L.az + x] = th[L.az + x - 1]; th[L.az + x - 1] = t;
+                }
+            }
+        }
+    }
+    double* out = a.theta_prop + (uint64_t)q * PCS_MAX_P;
+    for (uint32_t p = 0; p < P; ++p) out[p] = th[p];
+
+    /* forward-model arguments (simulation_impl.inl:293-340) */
+    PropDev pd;
+    pd.job = j;
+    pd.slot = slot;
+    pd.trial = trial;
+    pd.gen = gen;
+    pd.quirk_full_az = 0u;
+    double powc[PCS_MAX_C], csum = 0.0;
+    for (uint32_t i = 0; i < L.C; ++i) {
+        powc[i] = pow(10.0, th[L.c + i]);
+        csum += powc[i];
+    }
+    double acc = 0.0;
+    for (uint32_t i = 0; i < PCS_MAX_C; ++i) {
+        pd.pre_comp_prob[i] = 2.0f;
+        pd.sd_scale[i] = 0.0f;
+        pd.sd_shape[i] = 0.0f;
+        pd.half_az[i] = 0.0f;
+    }
+    for (uint32_t i = 0; i < L.C; ++i) {
+        acc += powc[i] / csum;
+        pd.pre_comp_prob[i] = (float)acc;
+        if (pm.model == PCS_DEV_MODEL_LOGNORMAL) {
+            /* lognormal diameter (nm) with mean mu, sd s: sigma_ln^2 = ln(1 + s^2/mu^2) */
+            const double mu = th[L.m + i], sdv = th[L.s + i];
+            const double sl2 = log1p((sdv * sdv) / (mu * mu));
+            const double mul = log(mu) - 0.5 * sl2;
+            pd.sd_scale[i] = (float)(pm.sd_const * exp(-0.5 * mul));
+            pd.sd_shape[i] = (float)(-0.5 * sqrt(sl2));
+        } else {
+            pd.sd_scale[i] = (float)sqrt(2.0 * th[L.m + i] * pm.delta_t);
+        }
+    }
+    pd.pre_comp_prob[L.C - 1] = 2.0f; /* simulation_impl.inl:331-335 */
+    for (uint32_t z = 0; z < L.Z; ++z) {
+        const float azf = (float)th[L.az + z];
+        pd.half_az[z] = (gen == 0u && pm.quirk_full_az) ? azf : 0.5f * azf;
+    }
+    const double lambda = csum * pm.volume_factor;
+
+    /* particle counts and their prefix */
+    const uint64_t coff = (uint64_t)q * (2u * rd->v_max + 1u);
+    uint32_t* cnt = a.counts + coff;
+    uint32_t* pre = cnt + jd.V;
+    uint64_t total = 0, steps = 0;
+    pre[0] = 0u;
+    for (uint32_t v = 0; v < jd.V; ++v) {
+        const uint32_t c = poisson_(lambda, v, slot, gt, k0, k1);
+        cnt[v] = c;
+        total += c;
+        steps += (uint64_t)c * jd.frames[v];
+        pre[v + 1] = (uint32_t)min(total, (uint64_t)0xFFFFFFFFu);
+    }
+    if (total > 0xFFFFFFFFull) atomicOr(a.err, PCS_ERRBIT_COUNTS);
+    pd.total_particles = (uint32_t)min(total, (uint64_t)0xFFFFFFFFu);
+    pd.counts_off = coff;
+    pd.hist_off = rd->job_hist_base[j] + (uint64_t)local * ((uint64_t)jd.R * jd.B);
+    pd.item_count = (pd.total_particles + rd->chunk - 1u) / rd->chunk;
+    pd.item_begin = 0u;
+    a.props[q] = pd;
+    atomicAdd((unsigned long long*)&pm.particle_steps, (unsigned long long)steps);
+}
+
+/* ----------------------------------------------------------------------- */
+/* item scan: one block */
+__global__ void __launch_bounds__(1024) k_items(PmcArgs a)
+{
+    __shared__ uint32_t s_part[1024];
+    RoundDev* rd = a.round;
+    const uint32_t M = rd->n_props;
+    const uint32_t per = (M + blockDim.x - 1) / blockDim.x;
+    const uint32_t b = threadIdx.x * per, e = min(b + per, M);
+    uint32_t sum = 0;
+    for (uint32_t q = b; q < e; ++q) sum += a.props[q].item_count;
+    s_part[threadIdx.x] = sum;
+    __syncthreads();
+    for (uint32_t d = 1; d < blockDim.x; d <<= 1) {
+        uint32_t t = (threadIdx.x >= d) ? s_part[threadIdx.x - d] : 0u;
+        __syncthreads();
+        s_part[threadIdx.x] += t;
+        __syncthreads();
+    }
+    uint32_t run = s_part[threadIdx.x] - sum;
+    for (uint32_t q = b; q < e; ++q) {
+        a.props[q].item_begin = run;
+        run += a.props[q].item_count;
+    }
+    const uint32_t total = s_part[blockDim.x - 1];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (total > rd->items_cap) atomicOr(a.err, PCS_ERRBIT_ITEMS);
+        rd->n_items = min(total, rd->items_cap);
+        rd->queue_head = 0u;
+    }
+    for (uint32_t q = b; q < e; ++q) {
+        const uint32_t ib = a.props[q].item_begin, ic = a.props[q].item_count;
+        for (uint32_t i = 0; i < ic; ++i)
+            if (ib + i < rd->items_cap) a.item_prop[ib + i] = q;
+    }
+}
+
+/* ----------------------------------------------------------------------- */
+/* accept: one block per job */
+__global__ void __launch_bounds__(1024) k_accept(PmcArgs a)
+{
+    __shared__ uint32_t s_keep;
+    __shared__ unsigned long long s_trials, s_acc;
+    const uint32_t j = blockIdx.x;
+    RoundDev* rd = a.round;
+    if (j >= rd->n_jobs) return;
+    JobPmcDev& pm = a.pmc[j];
+    if (pm.done) return;
+    const uint32_t k = rd->job_k[j];
+    const uint32_t cnt = rd->job_count[j];
+    const uint32_t base = rd->job_base[j];
+    const uint32_t nprop_slots = cnt / k;
+    const uint32_t npend = pm.pending_count;
+    const uint32_t P = pm.P;
+    if (threadIdx.x == 0) {
+        s_keep = 0u;
+        s_trials = 0ull;
+        s_acc = 0ull;
+        pm.gen_ended = 0u;
+    }
+    __syncthreads();
+    /* decide every pending slot; kept slots go to scratch (as u32 bits) */
+    uint32_t* keep_list = reinterpret_cast<uint32_t*>(pm.scratch);
+    for (uint32_t i = threadIdx.x; i < npend; i += blockDim.x) {
+        const uint32_t slot = pm.pending[i];
+        bool acc_ok = false;
+        if (i < nprop_slots) {
+            uint32_t first = k;
+            double dsel = 0.0;
+            for (uint32_t r = 0; r < k; ++r) {
+                const uint32_t q = base + i * k + r;
+                const double df = a.use_f64_distance && a.dist_f64 ? a.dist_f64[q] : (double)a.dist_f32[q];
+                const double d = log10(df);
+                if (pm.generation == 0u || d <= pm.gamma) {
+                    first = r;
+                    dsel = d;
+                    break;
+                }
+            }
+            if (first < k) {
+                const uint32_t q = base + i * k + first;
+                for (uint32_t p = 0; p < P; ++p)
+                    pm.theta_new[(uint64_t)slot * P + p] = a.theta_prop[(uint64_t)q * PCS_MAX_P + p];
+                pm.dist_new[slot] = dsel;
+                pm.accepted[slot] = 1u;
+                acc_ok = true;
+                atomicAdd(&s_trials, (unsigned long long)(first + 1u));
+                atomicAdd(&s_acc, 1ull);
+            } else {
+                pm.next_trial[slot] += k;
+                atomicAdd(&s_trials, (unsigned long long)k);
+            }
+        }
+        if (!acc_ok) keep_list[atomicAdd(&s_keep, 1u)] = slot;
+    }
+    __syncthreads();
+    const uint32_t nk = s_keep;
+    for (uint32_t i = threadIdx.x; i < nk; i += blockDim.x) pm.pending[i] = keep_list[i];
+    if (threadIdx.x == 0) {
+        pm.pending_count = nk;
+        pm.trials += s_trials;
+        pm.simulations += cnt;
+        pm.accepted_total += s_acc;
+        const bool cap = pm.generation > 0u &&
+                         (double)pm.trials >= (double)pm.avg_trials * (double)pm.N;
+        if (nk == 0u || cap) pm.gen_ended = 1u;
+    }
+}
+
+/* ----------------------------------------------------------------------- */
+/* whitened coordinates for the kernel density: y = A^-1 (theta - mean),
+ * A = diag(tau) or the Cholesky factor; fixed parameters dropped.  Output
+ * float [2][N][P] in the job's ybuf (old population, then new). */
+__global__ void k_whiten(PmcArgs a)
+{
+    const uint32_t j = blockIdx.y;
+    if (j >= a.round->n_jobs) return;
+    JobPmcDev& pm = a.pmc[j];
+    if (pm.done || !pm.gen_ended || pm.generation == 0u || pm.weighting != 0u) return;
+    if ((double)pm.trials >= (double)pm.avg_trials * (double)pm.N) return;
+    const uint32_t N = pm.N, P = pm.P;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2u * N) return;
+    const double* th = (i < N) ? pm.theta + (uint64_t)i * P : pm.theta_new + (uint64_t)(i - N) * P;
+    float* y = pm.ybuf + (uint64_t)i * P;
+    double v[PCS_MAX_P];
+    for (uint32_t p = 0; p < P; ++p) v[p] = th[p] - pm.lo[p];
+    if (pm.perturbation == 1u) {
+        for (uint32_t p = 0; p < P; ++p) {
+            if (pm.fixed[p]) {
+                v[p] = 0.0;
+                continue;
+            }
+            double s = v[p];
+            for (uint32_t q = 0; q < p; ++q)
+                if (!pm.fixed[q]) s -= pm.factor[p * P + q] * v[q];
+            v[p] = s / pm.factor[p * P + p];
+        }
+    } else {
+        for (uint32_t p = 0; p < P; ++p) v[p] = pm.fixed[p] ? 0.0 : v[p] / pm.factor[p * P + p];
+    }
+    for (uint32_t p = 0; p < P; ++p) y[p] = (float)v[p];
+}
+
+/* pmc-standard (simulation_impl.inl:832-871): log w*_a = -log sum_i w_i
+ * exp(-0.5 |y*_a - y_i|^2) (the Gaussian normalising constants cancel in
+ * the normalisation).  One warp per new particle a. */
+__global__ void __launch_bounds__(256) k_kernel_sum(PmcArgs a)
+{
+    const uint32_t j = blockIdx.y;
+    if (j >= a.round->n_jobs) return;
+    JobPmcDev& pm = a.pmc[j];
+    if (pm.done || !pm.gen_ended || pm.generation == 0u || pm.weighting != 0u) return;
+    if ((double)pm.trials >= (double)pm.avg_trials * (double)pm.N) return;
+    const uint32_t N = pm.N, P = pm.P;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t an = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (an >= N) return;
+    const float* yb = pm.ybuf;
+    const float* ya = yb + (uint64_t)(N + an) * P;
+    float yl[PCS_MAX_P];
+    for (uint32_t p = 0; p < P; ++p) yl[p] = ya[p];
+    /* pass 1: max exponent; pass 2: scaled sum */
+    float mx = -INFINITY;
+    for (uint32_t i = lane; i < N; i += 32u) {
+        if (!(pm.w[i] > 0.0)) continue;
+        const float* yi = yb + (uint64_t)i * P;
+        float s = 0.0f;
+        for (uint32_t p = 0; p < P; ++p) {
+            float d = yl[p] - yi[p];
+            s = fmaf(d, d, s);
+        }
+        mx = fmaxf(mx, -0.5f * s);
+    }
+    for (int d = 16; d >= 1; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, d));
+    float acc = 0.0f;
+    for (uint32_t i = lane; i < N; i += 32u) {
+        const float wi = (float)pm.w[i];
+        if (!(wi > 0.0f)) continue;
+        const float* yi = yb + (uint64_t)i * P;
+        float s = 0.0f;
+        for (uint32_t p = 0; p < P; ++p) {
+            float d = yl[p] - yi[p];
+            s = fmaf(d, d, s);
+        }
+        acc = fmaf(wi, __expf(-0.5f * s - mx), acc);
+    }
+    for (int d = 16; d >= 1; d >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, d);
+    if (lane == 0) pm.scratch[an] = -(double)mx - log((double)acc); /* log w*_a */
+}
+
+/* ----------------------------------------------------------------------- */
+/* rank of element i in (value, index) order */
+__device__ uint32_t select_rank_(const double* x, uint32_t N, uint32_t target, double* out_shared)
+{
+    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
+        const double xi = x[i];
+        uint32_t rank = 0;
+        for (uint32_t t = 0; t < N; ++t) {
+            const double xt = x[t];
+            rank += (xt < xi || (xt == xi && t < i)) ? 1u : 0u;
+        }
+        if (rank == target) *out_shared = xi;
+    }
+    return 0;
+}
+
+__device__ double block_sum_(double v, double* s_red)
+{
+    for (int d = 16; d >= 1; d >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, d);
+    const uint32_t w = threadIdx.x >> 5, l = threadIdx.x & 31u;
+    __syncthreads();
+    if (l == 0) s_red[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    const uint32_t nw = blockDim.x >> 5;
+    if (w == 0) {
+        t = (l < nw) ? s_red[l] : 0.0;
+        for (int d = 16; d >= 1; d >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, d);
+        if (l == 0) s_red[0] = t;
+    }
+    __syncthreads();
+    t = s_red[0];
+    __syncthreads();
+    return t;
+}
+
+__device__ double block_max_(double v, double* s_red)
+{
+    for (int d = 16; d >= 1; d >>= 1) v = fmax(v, __shfl_xor_sync(0xFFFFFFFFu, v, d));
+    const uint32_t w = threadIdx.x >> 5, l = threadIdx.x & 31u;
+    __syncthreads();
+    if (l == 0) s_red[w] = v;
+    __syncthreads();
+    const uint32_t nw = blockDim.x >> 5;
+    if (w == 0) {
+        double t = (l < nw) ? s_red[l] : -INFINITY;
+        for (int d = 16; d >= 1; d >>= 1) t = fmax(t, __shfl_xor_sync(0xFFFFFFFFu, t, d));
+        if (l == 0) s_red[0] = t;
+    }
+    __syncthreads();
+    double t = s_red[0];
+    __syncthreads();
+    return t;
+}
+
+/* start of a main iteration (simulation_impl.inl:202-222): count it, stop
+ * once -S is exceeded (the count then stays at max + 1, as the reference's
+ * meta reports), lower gamma on the delta schedule */
+__device__ void start_generation_(JobPmcDev& pm)
+{
+    pm.iterations += 1u;
+    if (pm.max_generations && pm.iterations > pm.max_generations) {
+        pm.done = 1u;
+        return;
+    }
+    if (pm.schedule == 0u) pm.gamma -= pm.delta_gamma;
+    pm.generation += 1u;
+    pm.pending_count = pm.N;
+    pm.trials = 0ull;
+    pm.gen_ended = 0u;
+}
+
+/* finalize: one block per job whose generation ended this round */
+__global__ void __launch_bounds__(1024) k_finalize(PmcArgs a)
+{
+    __shared__ double s_red[32];
+    __shared__ double s_sel;
+    __shared__ double s_mean[PCS_MAX_P];
+    __shared__ double s_cov[PCS_MAX_P * PCS_MAX_P];
+    const uint32_t j = blockIdx.x;
+    RoundDev* rd = a.round;
+    if (j >= rd->n_jobs) return;
+    JobPmcDev& pm = a.pmc[j];
+    if (pm.done || !pm.gen_ended) return;
+    const uint32_t N = pm.N, P = pm.P;
+    const uint32_t tid = threadIdx.x, bd = blockDim.x;
+
+    bool commit = true;
+    if (pm.generation == 0u) {
+        /* prior pass: gamma_0 from the median distance (compute_initial_gamma_ :819-829) */
+        if (tid == 0) s_sel = 0.0;
+        __syncthreads();
+        const uint32_t target = (pm.schedule == 1u) ? min(N - 1u, (uint32_t)floor(pm.quantile * N)) : N / 2u;
+        select_rank_(pm.dist_new, N, target, &s_sel);
+        __syncthreads();
+        if (tid == 0) pm.gamma = s_sel;
+        /* the reference keeps the prior population as drawn; the quantile
+         * schedule keeps its distances as the generation-0 distances */
+        for (uint32_t i = tid; i < N; i += bd) pm.dist[i] = (pm.schedule == 1u) ? pm.dist_new[i] : 0.0;
+        commit = false;
+    } else if ((double)pm.trials >= (double)pm.avg_trials * (double)pm.N) {
+        /* trial cap: converged, discard this generation (:425-428) */
+        if (tid == 0) {
+            pm.converged = 1u;
+            pm.done = 1u;
+        }
+        return;
+    }
+
+    if (commit) {
+        /* weights */
+        if (pm.weighting == 0u) {
+            double mx = -INFINITY;
+            for (uint32_t i = tid; i < N; i += bd) mx = fmax(mx, pm.scratch[i]);
+            mx = block_max_(mx, s_red);
+            double s = 0.0;
+            for (uint32_t i = tid; i < N; i += bd) {
+                const double e = exp(pm.scratch[i] - mx);
+                pm.scratch[i] = e;
+                s += e;
+            }
+            s = block_sum_(s, s_red);
+            for (uint32_t i = tid; i < N; i += bd) pm.w[i] = pm.scratch[i] / s;
+        } else {
+            /* inverse-distance-squared (:872-887) */
+            double s = 0.0;
+            for (uint32_t i = tid; i < N; i += bd) {
+                const double d = pm.dist_new[i];
+                const double wv = 1.0 / (d * d);
+                pm.scratch[i] = wv;
+                s += wv;
+            }
+            s = block_sum_(s, s_red);
+            for (uint32_t i = tid; i < N; i += bd) pm.w[i] = pm.scratch[i] / s;
+        }
+        /* commit the new population (:434-450) */
+        for (uint64_t i = tid; i < (uint64_t)N * P; i += bd) pm.theta[i] = pm.theta_new[i];
+        for (uint32_t i = tid; i < N; i += bd) pm.dist[i] = pm.dist_new[i];
+        __syncthreads();
+    }
+
+    /* cumulative weights (partial_sum, :222); single thread keeps the order */
+    if (tid == 0) {
+        double acc = 0.0;
+        for (uint32_t i = 0; i < N; ++i) {
+            acc += pm.w[i];
+            pm.wcum[i] = acc;
+        }
+    }
+    /* perturbation factor from the (new) committed population */
+    if (pm.perturbation == 0u) {
+        /* compute_tau_ (:733-749): tau = sqrt(2 var), uncorrected 1/N variance */
+        for (uint32_t p = 0; p < P; ++p) {
+            double s = 0.0;
+            for (uint32_t i = tid; i < N; i += bd) s += pm.theta[(uint64_t)i * P + p];
+            s = block_sum_(s, s_red);
+            const double mean = s / (double)N;
+            double v = 0.0;
+            for (uint32_t i = tid; i < N; i += bd) {
+                const double x = pm.theta[(uint64_t)i * P + p] - mean;
+                v += x * x;
+            }
+            v = block_sum_(v, s_red);
+            if (tid == 0) {
+                for (uint32_t q = 0; q < P; ++q) pm.factor[p * P + q] = 0.0;
+                pm.factor[p * P + p] = sqrt(2.0 * (v / (double)N));
+            }
+        }
+    } else {
+        /* 2 x weighted covariance and its Cholesky factor (Beaumont et al. 2009) */
+        for (uint32_t p = 0; p < P; ++p) {
+            double s = 0.0;
+            for (uint32_t i = tid; i < N; i += bd) s += pm.w[i] * pm.theta[(uint64_t)i * P + p];
+            s = block_sum_(s, s_red);
+            if (tid == 0) s_mean[p] = s;
+        }
+        __syncthreads();
+        for (uint32_t p = 0; p < P; ++p)
+            for (uint32_t q = 0; q <= p; ++q) {
+                double s = 0.0;
+                for (uint32_t i = tid; i < N; i += bd) {
+                    const double* t = pm.theta + (uint64_t)i * P;
+                    s += pm.w[i] * (t[p] - s_mean[p]) * (t[q] - s_mean[q]);
+                }
+                s = block_sum_(s, s_red);
+                if (tid == 0) s_cov[p * P + q] = s_cov[q * P + p] = 2.0 * s;
+            }
+        __syncthreads();
+        if (tid == 0) {
+            for (uint32_t x = 0; x < P * P; ++x) pm.factor[x] = 0.0;
+            for (uint32_t c = 0; c < P; ++c) {
+                if (pm.fixed[c]) continue;
+                double d = s_cov[c * P + c];
+                for (uint32_t t = 0; t < c; ++t)
+                    if (!pm.fixed[t]) d -= pm.factor[c * P + t] * pm.factor[c * P + t];
+                const double lv = sqrt(fmax(d, 1e-300));
+                pm.factor[c * P + c] = lv;
+                for (uint32_t r = c + 1; r < P; ++r) {
+                    if (pm.fixed[r]) continue;
+                    double s = s_cov[r * P + c];
+                    for (uint32_t t = 0; t < c; ++t)
+                        if (!pm.fixed[t]) s -= pm.factor[r * P + t] * pm.factor[c * P + t];
+                    pm.factor[r * P + c] = s / lv;
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    /* epsilon for the next generation */
+    if (pm.schedule == 1u && pm.generation > 0u) {
+        if (tid == 0) s_sel = 0.0;
+        __syncthreads();
+        const uint32_t target = min(N - 1u, (uint32_t)floor(pm.quantile * N));
+        select_rank_(pm.dist, N, target, &s_sel);
+        __syncthreads();
+    }
+    if (tid == 0) {
+        if (pm.schedule == 1u && pm.generation > 0u) pm.gamma = s_sel;
+        start_generation_(pm);
+    }
+    for (uint32_t i = tid; i < N; i += bd) {
+        pm.pending[i] = i;
+        pm.next_trial[i] = 0u;
+        pm.accepted[i] = 0u;
+    }
+}
+
+/* ----------------------------------------------------------------------- */
+/* observed cumulative histogram (simulation_impl.inl:605-629) */
+__global__ void k_observed_bin(const uint32_t* K, const double* DE, size_t n, uint32_t rows,
+                               uint32_t bins, double ub_de, uint32_t* sat, uint32_t* err)
+{
+    const double width = ub_de / (double)bins;
+    const uint64_t total = (uint64_t)rows * bins;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double de = DE[i];
+        if (de >= ub_de) continue;
+        const long long idx = (long long)(de / width);
+        const long long flat = (long long)K[i] * bins + idx;
+        if (flat < 0 || (unsigned long long)flat >= total) {
+            atomicOr(err, PCS_ERRBIT_HIST_BOUNDS);
+            continue;
+        }
+        atomicAdd(sat + flat, 1u);
+    }
+}
+
+/* column-wise then row-wise partial sums; also writes the transpose */
+__global__ void k_observed_cols(uint32_t rows, uint32_t bins, uint32_t* sat)
+{
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= bins) return;
+    uint32_t acc = 0;
+    for (uint32_t r = 0; r < rows; ++r) {
+        acc += sat[(uint64_t)r * bins + c];
+        sat[(uint64_t)r * bins + c] = acc;
+    }
+}
+
+__global__ void k_observed_rows(uint32_t rows, uint32_t bins, uint32_t* sat, uint32_t* sat_t)
+{
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    uint32_t acc = 0;
+    for (uint32_t c = 0; c < bins; ++c) {
+        acc += sat[(uint64_t)r * bins + c];
+        sat[(uint64_t)r * bins + c] = acc;
+        if (sat_t) sat_t[(uint64_t)c * rows + r] = acc;
+    }
+}
+
+/* ----------------------------------------------------------------------- */
+cudaError_t launch_round_plan(const PmcArgs& a, cudaStream_t st)
+{
+    k_round_plan<<<1, 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_propose(const PmcArgs& a, uint32_t capacity, cudaStream_t st)
+{
+    k_propose<<<(capacity + 127) / 128, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_items(const PmcArgs& a, cudaStream_t st)
+{
+    k_items<<<1, 1024, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accept(const PmcArgs& a, uint32_t n_jobs, cudaStream_t st)
+{
+    k_accept<<<n_jobs, 1024, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const PmcArgs& a, uint32_t n_jobs, uint32_t max_n, cudaStream_t st)
+{
+    dim3 gw((2u * max_n + 255) / 256, n_jobs);
+    k_whiten<<<gw, 256, 0, st>>>(a);
+    dim3 gk((max_n * 32u + 255) / 256, n_jobs);
+    k_kernel_sum<<<gk, 256, 0, st>>>(a);
+    k_finalize<<<n_jobs, 1024, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_observed_sat(const uint32_t* K, const double* DE, size_t n, uint32_t rows,
+                                uint32_t bins, double ub_de, uint32_t* sat, uint32_t* sat_t,
+                                uint32_t* err, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(sat, 0, sizeof(uint32_t) * (size_t)rows * bins, st);
+    if (e != cudaSuccess) return e;
+    if (n) k_observed_bin<<<(unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, st>>>(K, DE, n, rows, bins, ub_de, sat, err);
+    k_observed_cols<<<(bins + 127) / 128, 128, 0, st>>>(rows, bins, sat);
+    k_observed_rows<<<(rows + 127) / 128, 128, 0, st>>>(rows, bins, sat, sat_t);
+    return cudaGetLastError();
+}
+
+} // namespace pcs

@@ -1,0 +1,161 @@
+/*
+ * pcs_common.h -- types and counter-based random streams shared by the host
+ * engine and the sm_103a kernels.
+ *
+ * Layout in HBM (one GPU, everything device-resident for the life of a job):
+ *   per job        JobDev descriptor, observed cumulative histogram (R x B,
+ *                  row-major) and its transpose (B x R), frame counts [V],
+ *                  population theta [N x P] f64, weights/cumulative weights
+ *                  [N] f64, distances [N] f64, perturbation factor [P x P] f64,
+ *                  slot bookkeeping [N] u32.
+ *   per round      PropDev descriptors [M], proposed parameters [M x P] f64,
+ *                  particle counts [M x V] u32, histograms (sum of R_j*B_j
+ *                  over the round's proposals) u32, distances [M],
+ *                  work-item -> proposal map.
+ */
+#ifndef PCS_COMMON_H
+#define PCS_COMMON_H
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define PCS_HD __host__ __device__ __forceinline__
+#else
+#define PCS_HD inline
+#endif
+
+#define PCS_MAX_C 8           /* mixture components per job */
+#define PCS_MAX_P 32          /* parameters per job: 3*C + Z for the lognormal model */
+#define PCS_MAX_V 4096        /* videos per job */
+#define PCS_WARP 32
+
+/* models: the reference's two (shared/common.hpp:9-16) plus the per-particle
+ * lognormal diameter model with Stokes-Einstein diffusivity */
+enum pcs_model_e {
+    PCS_DEV_MODEL_FIXED_Z = 0,
+    PCS_DEV_MODEL_VARIABLE_Z = 1,
+    PCS_DEV_MODEL_LOGNORMAL = 2
+};
+
+/* Stream tags (top byte of counter word 1): every random draw of a job is
+ * Philox4x32-10(counter, key = job seed) with a counter that names what the
+ * draw is for, so a draw depends only on (seed, generation, slot, trial,
+ * particle, step) and never on how work is scheduled or batched. */
+enum pcs_stream_e {
+    PCS_STREAM_PARTICLE = 0x0u,  /* c0 particle, c1 block j (0 position, 1 size, 2+ steps) */
+    PCS_STREAM_POISSON = 0x1u,   /* c0 video */
+    PCS_STREAM_PERTURB = 0x2u,   /* c0 parameter pair */
+    PCS_STREAM_PICK = 0x3u,      /* c0 0 */
+    PCS_STREAM_PRIOR = 0x4u      /* c0 parameter pair */
+};
+
+/* ----------------------------------------------------------------------- */
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11, "Parallel random      */
+/* numbers: as easy as 1, 2, 3"): 10 rounds of the published S-box with    */
+/* the published multipliers and Weyl key increments.                       */
+/* ----------------------------------------------------------------------- */
+struct pcs_u4 {
+    uint32_t x, y, z, w;
+};
+
+PCS_HD void pcs_mulhilo(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo)
+{
+#if defined(__CUDA_ARCH__)
+    *hi = __umulhi(a, b);
+    *lo = a * b;
+#else
+    uint64_t p = (uint64_t)a * b;
+    *hi = (uint32_t)(p >> 32);
+    *lo = (uint32_t)p;
+#endif
+}
+
+PCS_HD pcs_u4 pcs_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1)
+{
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0, lo0, hi1, lo1;
+        pcs_mulhilo(0xD2511F53u, c0, &hi0, &lo0);
+        pcs_mulhilo(0xCD9E8D57u, c2, &hi1, &lo1);
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    pcs_u4 o = {c0, c1, c2, c3};
+    return o;
+}
+
+/* counter word 3: generation (12 bits) and trial (20 bits) */
+PCS_HD uint32_t pcs_ctr_gen_trial(uint32_t gen, uint32_t trial)
+{
+    return (gen << 20) | (trial & 0xFFFFFu);
+}
+
+PCS_HD uint32_t pcs_ctr_tag(uint32_t tag, uint32_t j)
+{
+    return (tag << 28) | (j & 0x0FFFFFFFu);
+}
+
+/* 24-bit uniform in [0,1): exact float, as the parity fixtures use */
+PCS_HD float pcs_u01_24(uint32_t r)
+{
+    return (float)(r >> 8) * (1.0f / 16777216.0f);
+}
+
+/* 53-bit uniform in [0,1) from two words */
+PCS_HD double pcs_u01_53(uint32_t a, uint32_t b)
+{
+    uint64_t m = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
+    return (double)m * (1.0 / 9007199254740992.0);
+}
+
+/* ----------------------------------------------------------------------- */
+/* Device-resident descriptors                                             */
+/* ----------------------------------------------------------------------- */
+
+/* Per-job constants read by the forward model and the distance kernel.
+ * Float fields are formed on the host exactly as the reference forms its
+ * SimulateSetup (detail/simulation_impl.inl:568-579): 0.5f * float(x). */
+struct JobDev {
+    float half_lx, half_ly, half_lz;
+    float half_ax, half_ay;
+    float four_delta_t;
+    float dde;             /* float(double(ub_de) / B) */
+    uint32_t kmin;
+    uint32_t V, R, B;
+    uint32_t model, C, Z, P;
+    uint32_t seed_lo, seed_hi;
+    uint32_t frames_max;
+    uint32_t pad0;
+    const uint32_t* frames;     /* [V] */
+    const uint32_t* ref_sat;    /* [R*B] observed cumulative histogram */
+    const uint32_t* ref_sat_t;  /* [B*R] transposed copy, for column sweeps */
+};
+
+/* Per-proposal forward-model arguments (the SimulateRun of one proposal,
+ * detail/simulation_impl.inl:319-340) plus its place in the round. */
+struct PropDev {
+    uint32_t job;          /* index into the round's job table */
+    uint32_t slot;         /* population slot the proposal is for */
+    uint32_t trial;        /* trial ordinal of the slot in this generation */
+    uint32_t gen;          /* generation */
+    uint32_t total_particles;
+    uint32_t item_begin;   /* first work item */
+    uint32_t item_count;
+    uint32_t quirk_full_az;/* unused by kernels; kept for layout */
+    uint64_t hist_off;     /* offset of this proposal's R x B histogram (u32 words) */
+    uint64_t counts_off;   /* offset of this proposal's [V] particle counts and [V+1] prefix */
+    float half_az[PCS_MAX_C];
+    float pre_comp_prob[PCS_MAX_C];
+    float sd_scale[PCS_MAX_C]; /* discrete: float(sqrt(2 m dt)); lognormal: step sd at z = 0 */
+    float sd_shape[PCS_MAX_C]; /* lognormal: -0.5 * sigma_ln; discrete: 0 */
+};
+
+#endif

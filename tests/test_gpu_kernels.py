@@ -1,0 +1,166 @@
+"""Parity of the sm_103a kernels with the oracle, through the C ABI.
+
+Bit-exact: forward-model histograms on replayed draws (golden fixtures made
+by the reference's own kernel code), prefix sums, float and double distances
+in the reference reduction order, exact sums of squares, observed cumulative
+histograms, raw Philox words.  Statistical: histograms on the product's own
+random streams against the oracle on the same streams."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_replay_cases
+
+pytestmark = pytest.mark.gpu
+
+
+def fwd(pcs, st, lognormal=None):
+    setup = pcs.ForwardSetup(st.model if lognormal is None else 2, st.C, st.frames, st.kmin, st.four_delta_t,
+                             st.half_l, st.half_a, st.dde, st.R, st.B)
+    run = pcs.ForwardRun(st.particles, st.half_az, st.pre_comp_prob, st.rwsd if lognormal is None else lognormal[0],
+                         None if lognormal is None else lognormal[1])
+    return setup, run
+
+
+@pytest.mark.parametrize("tile_rows", [0, 16, 4096])
+def test_replay_golden_bit_exact(pcs, ctx, oracle, tile_rows):
+    ctx.set_tuning(hist_tile_rows=tile_rows if tile_rows else 0xFFFFFFFF)
+    try:
+        for name, st, seed, gold in load_replay_cases(oracle):
+            u, z, _ = oracle.replay_draws(seed, st.n_particles, st.stride)
+            setup, run = fwd(pcs, st)
+            got = pcs.simulate_hist(ctx, setup, run, replay=(u, z, None))[0]
+            assert np.array_equal(got, gold), (name, int(got.sum()), int(gold.sum()))
+    finally:
+        ctx.set_tuning(hist_tile_rows=64)
+
+
+def test_replay_lognormal_bit_exact(pcs, ctx, oracle):
+    st = oracle.Setup(2, 2, np.array([80, 64, 90], np.uint32), np.array([70, 0, 55], np.uint32), 2, 0.2,
+                      (10.0, 8.0, 2.0), (5.0, 4.0), np.array([0.75], np.float32),
+                      np.array([0.4, 2.0], np.float32), np.zeros(2, np.float32), 0.1, 91, 40)
+    u, z, sig = oracle.replay_draws(17, st.n_particles, st.stride, with_sigmas=True, base_sigma=0.5)
+    want, _ = oracle.simulate_replay(st, u, z, sig)
+    setup, run = fwd(pcs, st, lognormal=(np.array([0.4, 0.4], np.float32), np.zeros(2, np.float32)))
+    got = pcs.simulate_hist(ctx, setup, run, replay=(u, z, sig))[0]
+    assert want.sum() > 0 and np.array_equal(got, want)
+
+
+def test_distance_golden_bit_exact(pcs, ctx):
+    zf = np.load(os.path.join(GOLDEN, "distance_cases.npz"))
+    for i in range(int(zf["count"][0])):
+        h, ref = zf[f"c{i}_hist"], zf[f"c{i}_ref"]
+        r = pcs.scan_distance(ctx, h, ref, want_cum=True, want_f64=True, want_ssd=True)
+        assert r["dist_f32"][0].tobytes() == zf[f"c{i}_dist"][0].tobytes(), i
+        assert r["dist_f64"][0] == zf[f"c{i}_dist64"][0], i
+        assert np.array_equal(r["cum"][0], zf[f"c{i}_cum"]), i
+        hi, lo = zf[f"c{i}_ssd"]
+        assert r["ssd"][0] == (int(hi) << 64) | int(lo), i
+
+
+def test_distance_batch_and_sizes(pcs, ctx, oracle):
+    rng = np.random.default_rng(8)
+    for R, B in [(301, 128), (513, 7), (1001, 256), (2, 300)]:
+        n = 3
+        hist = rng.poisson(0.7, (n, R, B)).astype(np.uint32)
+        ref = np.cumsum(np.cumsum(rng.poisson(0.7, (R, B)), 0), 1).astype(np.uint32)
+        r = pcs.scan_distance(ctx, hist, ref, want_ssd=True)
+        for q in range(n):
+            d, _, ssd = oracle.distance_kdist(hist[q], ref)
+            assert r["dist_f32"][q].tobytes() == np.float32(d).tobytes(), (R, B, q)
+            assert r["ssd"][q] == ssd
+
+
+def test_observed_sat_matches_oracle(pcs, ctx, oracle):
+    rng = np.random.default_rng(5)
+    R, B, ub = 1001, 1000, 5.0
+    K = rng.integers(3, 1000, 38302)
+    DE = rng.gamma(2.0, 0.6, 38302)
+    np.testing.assert_array_equal(pcs.observed_sat(ctx, K, DE, R, B, ub), oracle.observed_sat(K, DE, R, B, ub))
+
+
+def test_philox_stream_layout(pcs, ctx, oracle):
+    for seed, slot, trial, gen, n, blk in [(0, 0, 0, 0, 0, 0), (0xDEADBEEF12345678, 17, 3, 5, 999, 2),
+                                           (42, 4095, 0xFFFFF, 4095, 123456, 77)]:
+        got = pcs.debug_particle_stream(ctx, seed, slot, trial, gen, n, blk)
+        ctr = [n, (0 << 28) | blk, slot, (gen << 20) | trial]
+        want = oracle.philox(ctr, [seed & 0xFFFFFFFF, seed >> 32])
+        assert np.array_equal(got, want)
+
+
+def _cfg0_setup(oracle, V=20, frames=200, parts=128, C=1):
+    pc = np.array([2.0] if C == 1 else [0.6, 2.0], np.float32)
+    rw = np.array([np.float32(np.sqrt(2 * 2.626 / 30))] + ([np.float32(np.sqrt(2 * 0.919 / 30))] if C == 2 else []),
+                  np.float32)
+    return oracle.Setup(0, C, np.full(V, frames, np.uint32), np.full(V, parts, np.uint32), 2,
+                        float(np.float32(4) * np.float32(1 / 30)), (100.0, 80.0, 10.0), (50.0, 40.0),
+                        np.array([1.0], np.float32), pc, rw, float(np.float32(20.0 / 100)), frames + 1, 100)
+
+
+def test_philox_forward_model_matches_oracle_streams(pcs, ctx, oracle):
+    """Same Philox streams on both sides; the GPU's fast-math Box-Muller
+    differs in the last bits, so the histograms agree to a fraction of a
+    percent, far inside Monte-Carlo noise."""
+    st = _cfg0_setup(oracle, C=2)
+    setup, run = fwd(pcs, st)
+    runs = []
+    for s in range(4):
+        r = pcs.ForwardRun(st.particles, st.half_az, st.pre_comp_prob, st.rwsd, slot=s, trial=1, generation=2)
+        runs.append(r)
+    got = pcs.simulate_hist(ctx, setup, runs, seed=12345)
+    for s in range(4):
+        want, _ = oracle.simulate_philox(st, 12345, slot=s, trial=1, generation=2)
+        tot = want.sum()
+        assert tot > 1000
+        assert abs(int(got[s].sum()) - int(tot)) <= 0.005 * tot + 5
+        assert np.abs(got[s].astype(np.int64) - want).sum() <= 0.02 * tot + 10
+
+
+def _moments(h):
+    R, B = h.shape
+    k = np.arange(R)[:, None]
+    b = np.arange(B)[None, :]
+    n = h.sum()
+    return n, (h * k).sum() / n, (h * b).sum() / n
+
+
+def test_fresh_draws_moments_within_3_se(pcs, ctx, oracle):
+    """Histogram moments of the GPU path within 3 Monte-Carlo standard errors
+    of the oracle's on independent draws at the same parameters."""
+    st = _cfg0_setup(oracle)
+    setup, run = fwd(pcs, st)
+    reps = 24
+    runs = [pcs.ForwardRun(st.particles, st.half_az, st.pre_comp_prob, st.rwsd, slot=s) for s in range(reps)]
+    g = pcs.simulate_hist(ctx, setup, runs, seed=1)
+    o = np.stack([oracle.simulate_philox(st, 99, slot=s)[0] for s in range(reps)])
+    for stat in range(3):
+        a = np.array([_moments(x)[stat] for x in g], float)
+        b = np.array([_moments(x)[stat] for x in o], float)
+        se = np.sqrt(a.var(ddof=1) / reps + b.var(ddof=1) / reps)
+        assert abs(a.mean() - b.mean()) <= 3 * se + 1e-9, (stat, a.mean(), b.mean(), se)
+
+
+def test_philox_determinism_and_independence(pcs, ctx, oracle):
+    st = _cfg0_setup(oracle, V=5, frames=120, parts=300)
+    setup, run = fwd(pcs, st)
+    a = pcs.simulate_hist(ctx, setup, [run, run], seed=7)
+    b = pcs.simulate_hist(ctx, setup, [run], seed=7)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], a[0])
+    c = pcs.simulate_hist(ctx, setup, [run], seed=8)
+    assert not np.array_equal(b[0], c[0])
+    # independent of the launch shape
+    for kw in [dict(block_size=128, particles_per_thread=1), dict(block_size=512, particles_per_thread=2),
+               dict(block_size=256, particles_per_thread=4, warp_aggregate=1)]:
+        ctx.set_tuning(**kw)
+        d = pcs.simulate_hist(ctx, setup, [run], seed=7)
+        assert np.array_equal(d[0], b[0]), kw
+    ctx.set_tuning(block_size=256, particles_per_thread=1, warp_aggregate=0xFFFFFFFF)
+
+
+def test_bad_arguments_raise(pcs, ctx, oracle):
+    st = _cfg0_setup(oracle, V=2, frames=10, parts=5)
+    setup, run = fwd(pcs, st)
+    setup.rows = 5  # rows must exceed the frame count
+    with pytest.raises(pcs.PcsError):
+        pcs.simulate_hist(ctx, setup, run)

@@ -1,0 +1,111 @@
+"""The oracle, pinned: against the reference's own kernel code (golden
+fixtures made by tests/golden/make_golden.py from oracle/_ref), against
+published Philox known-answer vectors, and against the restated distance."""
+import numpy as np
+import pytest
+
+from conftest import load_replay_cases
+
+
+def test_philox_known_answers(oracle):
+    # Random123 known-answer vectors for Philox4x32-10
+    assert [hex(x) for x in oracle.philox([0, 0, 0, 0], [0, 0])] == ["0x6627e8d5", "0xe169c58d", "0xbc57ac4c", "0x9b00dbd8"]
+    assert [hex(x) for x in oracle.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2)] == ["0x408f276d", "0x41c83b0e", "0xa20bc7c6", "0x6d5451fd"]
+    assert [hex(x) for x in oracle.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0])] == \
+        ["0xd16cfe09", "0x94fdcceb", "0x5001e420", "0x24126ea1"]
+
+
+def test_replay_matches_reference_golden(oracle):
+    cases = load_replay_cases(oracle)
+    assert len(cases) >= 8
+    for name, st, seed, gold in cases:
+        u, z, _ = oracle.replay_draws(seed, st.n_particles, st.stride)
+        hist, (closed, recorded) = oracle.simulate_replay(st, u, z)
+        assert np.array_equal(hist, gold), name
+        assert recorded >= hist.sum()  # records with k == 0 land in row 0 only when kmin == 0
+
+
+def test_replay_matches_reference_kernel_random(oracle):
+    """Fresh random configurations against the host-compiled reference kernel."""
+    if not oracle.ref_available():
+        pytest.skip("oracle/_ref not built (reference tree absent)")
+    rng = np.random.default_rng(3)
+    for trial in range(6):
+        model = trial % 2
+        C = 1 + trial % 3
+        V = 1 + trial
+        frames = rng.integers(1, 50, V).astype(np.uint32)
+        parts = rng.integers(0, 60, V).astype(np.uint32)
+        pc = np.cumsum(np.ones(C) / C).astype(np.float32)
+        pc[-1] = 2
+        Z = 1 if model == 0 else C
+        st = oracle.Setup(model, C, frames, parts, trial % 4, float(np.float32(0.2)), (6.0, 5.0, 1.5), (3.0, 2.5),
+                          np.linspace(0.4, 1.0, Z).astype(np.float32), pc,
+                          np.linspace(0.2, 0.6, C).astype(np.float32), float(np.float32(0.25)),
+                          int(frames.max()) + 1, 24)
+        u, z, _ = oracle.replay_draws(100 + trial, st.n_particles, st.stride)
+        h1, _ = oracle.simulate_replay(st, u, z)
+        h2 = oracle.ref_simulate_replay(st, u, z)
+        assert np.array_equal(h1, h2)
+
+
+def test_distance_golden(oracle):
+    import os
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "distance_cases.npz"))
+    for i in range(int(z["count"][0])):
+        d, cum, ssd = oracle.distance_kdist(z[f"c{i}_hist"], z[f"c{i}_ref"])
+        assert np.float32(d).tobytes() == z[f"c{i}_dist"][0].tobytes()
+        assert np.array_equal(cum, z[f"c{i}_cum"])
+        hi, lo = z[f"c{i}_ssd"]
+        assert ssd == (int(hi) << 64) | int(lo)
+        assert oracle.distance_kdist_f64(z[f"c{i}_hist"], z[f"c{i}_ref"]) == z[f"c{i}_dist64"][0]
+
+
+def test_distance_properties(oracle):
+    """Prefix sums equal numpy's; the exact sum of squares agrees with the
+    float sum within float rounding."""
+    rng = np.random.default_rng(11)
+    for R, B in [(5, 7), (64, 64), (100, 33)]:
+        h = rng.integers(0, 5, (R, B)).astype(np.uint32)
+        ref = np.cumsum(np.cumsum(rng.integers(0, 5, (R, B)), 0), 1).astype(np.uint32)
+        d, cum, ssd = oracle.distance_kdist(h, ref)
+        want = np.cumsum(np.cumsum(h.astype(np.uint64), 1), 0).astype(np.uint32)
+        assert np.array_equal(cum, want)
+        exact = float(((cum.astype(np.int64) - ref.astype(np.int64)) ** 2).sum())
+        assert ssd == int(exact)
+        assert abs(float(d) - exact) <= 1e-5 * exact + 1
+
+
+def test_observed_sat_matches_numpy(oracle):
+    rng = np.random.default_rng(2)
+    R, B, ub = 51, 40, 5.0
+    K = rng.integers(2, 50, 3000)
+    DE = rng.uniform(0, 6.0, 3000)
+    sat = oracle.observed_sat(K, DE, R, B, ub)
+    H = np.zeros((R, B), np.uint64)
+    w = ub / B
+    for k, de in zip(K, DE):
+        if de >= ub:
+            continue
+        H[k, int(de / w)] += 1
+    assert np.array_equal(sat, np.cumsum(np.cumsum(H, 0), 1).astype(np.uint32))
+
+
+def test_pmc_pieces(oracle):
+    rng = np.random.default_rng(4)
+    N, P = 20, 3
+    th = rng.normal(size=(N, P))
+    ths = rng.normal(size=(N, P))
+    w = rng.dirichlet(np.ones(N))
+    tau = np.sqrt(2 * th.var(0))
+    import ctypes as C
+    out = np.zeros(N)
+    P_ = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    oracle.lib().orc_weights_pmc_standard(P_(ths), P_(th), P_(w), P_(tau), None, N, P, P_(out))
+    ref = np.array([1 / sum(w[i] * np.prod([np.exp(-0.5 * ((ths[a, p] - th[i, p]) / tau[p]) ** 2) /
+                                             (np.sqrt(2 * np.pi) * tau[p]) for p in range(P)]) for i in range(N))
+                    for a in range(N)])
+    np.testing.assert_allclose(out, ref / ref.sum(), rtol=1e-12)
+    assert oracle.lib().orc_displace(0.5, 0.7, 0.0, 1.0) == pytest.approx(0.8)
+    assert oracle.lib().orc_displace(0.5, -0.9, 0.0, 1.0) == pytest.approx(0.4)
