@@ -157,7 +157,8 @@ int orc_simulate_replay(const orc_setup* s, const orc_run* r, const orc_replay* 
             if (s->component_count > 1) idx = wrand_index(u[3], s->component_count, r->pre_comp_prob);
             if (idx >= s->component_count) return -3; /* pre_comp_prob must end above 1 */
 
-            float half_az = (s->model == ORC_MODEL_DISCRETE_FIXED_Z) ? r->half_az[0] : r->half_az[idx];
+            /* one depth for the fixed-depth and lognormal models, one per component otherwise */
+            float half_az = (s->model == ORC_MODEL_DISCRETE_VARIABLE_Z) ? r->half_az[idx] : r->half_az[0];
             float rwsd;
             if (s->model == ORC_MODEL_LOGNORMAL) {
                 if (!rp->sigmas) return -4;
