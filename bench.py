@@ -1,0 +1,296 @@
+#!/usr/bin/env python
+"""Benchmark of the ABC-PMC hot path on GB300.
+
+Workload (BASELINE configuration 1): two-component lognormal mixture
+(175/500 nm, sd 10/25 nm, weights 0.6/0.4, 5e14 m^-3), 50 videos x 300
+frames, population 1024, epsilon = 50% quantile, histograms 301 x 128.  A
+step is one ABC-PMC generation (batched rounds until every population slot
+has accepted a proposal).  The metric is particle-steps/s (one walk step of
+one particle; initial placements count as steps), whole job, all GPUs.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's CPU path (the Julia forward model of
+src/cpu/simulate.jl, restated in C as oracle/cpu_baseline.c because Julia
+is not installed) on all host cores, one bounded sample per step.  N > 1
+runs independent replicas (the path does not shard: no collectives).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# algorithmic thread-operations per particle-step of the forward model
+# (Philox 0.75 calls x 80, Box-Muller 1.5 pairs x 14, walk/detect/DE 32)
+OPS_PER_STEP = 113
+# bytes the distance kernel moves per histogram cell: read count, write zero,
+# read the observed cumulative histogram
+DIST_BYTES_PER_CELL = 12
+WORKLOAD = ("config1: 2-component lognormal (175/500 nm, sd 10/25, w 0.6/0.4), 5e14 m^-3, "
+            "50 videos x 300 frames, pop 1024, quantile-0.5 schedule, R x B = 301 x 128")
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(gpu_index)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is not None:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [l.strip().split(", ") for l in self.f.read().splitlines() if l.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def device_sm_count(P, device: int) -> int:
+    import ctypes
+    import re
+    buf = ctypes.create_string_buffer(1 << 16)
+    P.lib().pcs_device_report(buf, len(buf))
+    m = re.search(rf"^\s+{device + 1}: .*?, (\d+) SMs", buf.value.decode(), re.M)
+    return int(m.group(1)) if m else 152
+
+
+def dist_setup():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return rank, world, local
+
+
+def allreduce(x: float, op: str, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_job_dict(truth):
+    import part_conc_spt_abc_gb300.workloads as W
+    return dict(C=len(truth["mu"]), lognormal=1, m=truth["mu"], s=truth["sd"], c=truth["conc_ml"], az=[W.DEPTH],
+                temperature=W.T_K, viscosity=W.ETA, ax=W.AREA[0], ay=W.AREA[1], Lx=W.BOX[0], Ly=W.BOX[1],
+                Lz=W.BOX[2], deltat=W.DT, ub_de=W.UB_DE, kmin=2, B=128)
+
+
+def cpu_port_sample(target_s: float, threads: int):
+    """The reference CPU forward model on config-1 proposals at the true
+    parameters: a bounded sample sized to take about target_s seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    truth = dict(mu=[175.0, 500.0], sd=[10.0, 25.0], conc_ml=[3e8, 2e8])
+    job = cpu_job_dict(truth)
+    frames = np.full(50, 300, np.uint32)
+    steps, secs = O.cpu_forward_batch([job] * max(1, threads), frames, threads, seed=11)
+    rate = steps / max(secs, 1e-9)
+    per = steps / max(1, threads)
+    n = max(threads, int(target_s * rate / per))
+    return (lambda seed: O.cpu_forward_batch([job] * n, frames, threads, seed=seed)), n
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        barrier(world)
+        return
+    threads = os.cpu_count() or 1
+    sample, n = cpu_port_sample(3.0, threads)
+    for w in range(args.warmup):
+        sample(100 + w)
+    tot_steps, tot_s = 0, 0.0
+    for k in range(args.steps):
+        st, s = sample(200 + k)
+        tot_steps += st
+        tot_s += s
+    value = tot_steps / tot_s
+    line = {
+        "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": f"{n} forward simulations per step at the true parameters"},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} config-1 forward simulations per step, Julia conventions, Float64"},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="configuration 0 (pop 256): the case profiled under ncu")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import part_conc_spt_abc_gb300 as P
+    import part_conc_spt_abc_gb300.workloads as W
+
+    peaks, peak_src = measured_peaks()
+    ctx = P.Context(local)
+    gens = args.warmup + args.steps + 2
+    inp, truth = (W.config0 if args.small else W.config1)(ctx, seed=0, generations=gens)
+    tune = None
+    if not args.no_autotune:
+        t = ctx.autotune(inp)
+        tune = dict(block=t.block_size, ppt=t.particles_per_thread, tile_rows=t.hist_tile_rows,
+                    warp_aggregate=t.warp_aggregate, chunk=t.chunk_particles, capacity=t.round_capacity)
+
+    # ---- device-resident run: inputs already in HBM -----------------------
+    sim = P.make_simulation(ctx, inp, seed=1 + rank)
+    for _ in range(args.warmup):
+        sim.step()
+    barrier(world)
+    ctx.reset_kernel_stats()
+    i0 = sim.info()
+    clocks = Clocks(local)
+    ctx.timer_start()
+    for _ in range(args.steps):
+        sim.step()
+    ms = ctx.timer_stop()
+    clk = clocks.stop()
+    i1 = sim.info()
+    ks = ctx.kernel_stats()
+    steps_local = i1.particle_steps - i0.particle_steps
+    props_local = i1.simulations - i0.simulations
+    acc_local = i1.accepted - i0.accepted
+    ms_max = allreduce(ms, "max", world)
+    steps_all = allreduce(float(steps_local), "sum", world)
+    props_all = allreduce(float(props_local), "sum", world)
+    acc_all = allreduce(float(acc_local), "sum", world)
+    value = steps_all / (ms_max / 1e3)
+    sim.close()
+
+    # ---- end to end through the public API, host buffers ------------------
+    barrier(world)
+    t0 = time.perf_counter()
+    sim2 = P.make_simulation(ctx, inp, seed=101 + rank)  # H2D: observed K, DE, frame counts
+    d2h = 0
+    for _ in range(args.steps):
+        sim2.step()
+        out = sim2.output()  # D2H: the population (m, s, c, az, dist, w)
+        d2h = sum(a.nbytes for a in (out.m, out.c, out.az, out.dist, out.w, out.s) if a is not None)
+    e2e_s = time.perf_counter() - t0
+    e2e_steps = sim2.info().particle_steps
+    sim2.close()
+    e2e_s = allreduce(e2e_s, "max", world)
+    e2e_value = allreduce(float(e2e_steps), "sum", world) / e2e_s
+    h2d = (inp.K.nbytes + inp.DE.nbytes + inp.frames.nbytes) / args.steps
+
+    # ---- roofline of the dominant kernel (forward model: issue bound) -----
+    sim_ms = ks.simulate_ms / max(1, ks.simulate_launches)
+    steps_per_launch = ks.particle_steps / max(1, ks.simulate_launches)
+    achieved = steps_per_launch * OPS_PER_STEP / (sim_ms / 1e3) / 1e12
+    sm_count = device_sm_count(P, local)
+    peak = sm_count * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "simulate_config1_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    dist_ms = ks.distance_ms / max(1, ks.distance_launches)
+    dist_gbs = (ks.histogram_cells / max(1, ks.distance_launches)) * DIST_BYTES_PER_CELL / (dist_ms / 1e3) / 1e9
+
+    line = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "step": "one ABC-PMC generation", "parallelism": f"replicas x{world}",
+                   "l2": "working set above L2 (round histograms ~315 MB + job state)", "tuning": tune},
+        "proposals_per_s": props_all / (ms_max / 1e3),
+        "accepted_per_s": acc_all / (ms_max / 1e3),
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(ks.kernel_launches),
+        "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tops/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_simulate (fused forward model + histogram)",
+                     "achieved_def": f"{OPS_PER_STEP} algorithmic thread-ops per particle-step x steps per launch / launch time",
+                     "peak_def": f"{sm_count} SMs x 128 lanes x {peaks.get('sm_max_mhz', 2070.0)} MHz ({peak_src} clock)"},
+        "roofline_distance": {"bound": "hbm", "achieved": dist_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                              "frac": dist_gbs / float(peaks.get("hbm_gbs", 6800.0)),
+                              "kernel": "k_distance", "peak_src": peak_src},
+        "kernel_ms": {"simulate_per_launch": sim_ms, "distance_per_launch": dist_ms,
+                      "rounds": int(ks.rounds), "round_ms_total": ks.round_ms},
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample, n = cpu_port_sample(10.0, threads)
+        st, s = sample(7)
+        line["cpu_baseline"] = {"value": st / s, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                                "sample": f"{n} config-1 forward simulations (Julia conventions, Float64), {s:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    barrier(world)
+
+
+if __name__ == "__main__":
+    main()

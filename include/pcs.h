@@ -149,6 +149,27 @@ pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t);
 pcs_status pcs_autotune(pcs_ctx* ctx, const pcs_params* p, const pcs_observed* obs,
                         pcs_tuning* chosen);
 
+/* Device timeline: events on the context's stream (spans host gaps too). */
+pcs_status pcs_timer_start(pcs_ctx* ctx);
+pcs_status pcs_timer_stop(pcs_ctx* ctx, double* elapsed_ms);
+
+/* Per-kernel accounting of batched rounds, timed with CUDA events recorded
+ * around the launches inside the round graph. */
+typedef struct pcs_kernel_stats {
+    uint64_t rounds;
+    uint64_t kernel_launches;     /* all kernels of this library launched by rounds */
+    uint64_t simulate_launches;
+    double simulate_ms;           /* sum of forward-model launch durations */
+    uint64_t distance_launches;
+    double distance_ms;
+    double round_ms;              /* sum of round durations */
+    uint64_t proposals;           /* forward simulations */
+    uint64_t particle_steps;      /* walk steps incl. initial placements */
+    uint64_t histogram_cells;     /* R x B cells scanned by the distance kernel */
+} pcs_kernel_stats;
+pcs_status pcs_get_kernel_stats(pcs_ctx* ctx, pcs_kernel_stats* out);
+pcs_status pcs_reset_kernel_stats(pcs_ctx* ctx);
+
 /* ------------------------------------------------------------------ */
 /* Estimation jobs (Simulation, src/gpu/simulation.hpp:45-62)           */
 /* ------------------------------------------------------------------ */

@@ -53,6 +53,16 @@ class OrcCounts(C.Structure):
     _fields_ = [("closed", C.c_uint64), ("recorded", C.c_uint64)]
 
 
+class OrcCpuJob(C.Structure):
+    _fields_ = [
+        ("C", C.c_uint32), ("lognormal", C.c_int32), ("m", C.c_double * MAXC), ("s", C.c_double * MAXC),
+        ("c", C.c_double * MAXC), ("az", C.c_double * MAXC), ("temperature", C.c_double),
+        ("viscosity", C.c_double), ("ax", C.c_double), ("ay", C.c_double), ("Lx", C.c_double),
+        ("Ly", C.c_double), ("Lz", C.c_double), ("deltat", C.c_double), ("ub_de", C.c_double),
+        ("kmin", C.c_uint32), ("B", C.c_uint32), ("V", C.c_uint32), ("frames", _u32p),
+    ]
+
+
 def build(quiet: bool = True) -> None:
     """Compile the oracle (and, when the reference tree is present, oracle/_ref)."""
     out = subprocess.DEVNULL if quiet else None
@@ -99,8 +109,35 @@ def lib():
         L.orc_simulate_julia.restype = C.c_int
         L.orc_distance_julia.argtypes = [_i64p, _i64p, C.c_uint32, C.c_uint32]
         L.orc_distance_julia.restype = C.c_double
+        L.orc_cpu_forward_batch.argtypes = [C.POINTER(OrcCpuJob), C.c_uint32, C.c_uint32, C.c_uint64,
+                                            C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
+        L.orc_cpu_forward_batch.restype = C.c_uint64
         _lib = L
     return _lib
+
+
+def cpu_forward_batch(jobs, frames, nthreads: int, seed: int = 1):
+    """Times the Julia-convention forward model over `jobs` (list of dicts
+    with C, lognormal, m, s, c, az, temperature, viscosity, ax, ay, Lx, Ly,
+    Lz, deltat, ub_de, kmin, B) on nthreads threads.  Returns (steps, seconds)."""
+    fr = np.ascontiguousarray(frames, np.uint32)
+    arr = (OrcCpuJob * len(jobs))()
+    for i, j in enumerate(jobs):
+        a = arr[i]
+        a.C, a.lognormal = j["C"], int(j.get("lognormal", 0))
+        for k in range(j["C"]):
+            a.m[k], a.c[k] = j["m"][k], j["c"][k]
+            a.s[k] = j.get("s", [0.0] * MAXC)[k]
+        for k, v in enumerate(j["az"]):
+            a.az[k] = v
+        for f in ["temperature", "viscosity", "ax", "ay", "Lx", "Ly", "Lz", "deltat", "ub_de"]:
+            setattr(a, f, float(j.get(f, 0.0)))
+        a.kmin, a.B, a.V = j["kmin"], j["B"], len(fr)
+        a.frames = ptr(fr, C.c_uint32)
+    secs = C.c_double(0)
+    cs = C.c_uint64(0)
+    steps = lib().orc_cpu_forward_batch(arr, len(jobs), nthreads, seed, C.byref(secs), C.byref(cs))
+    return int(steps), float(secs.value)
 
 
 def ref_available() -> bool:

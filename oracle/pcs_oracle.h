@@ -160,6 +160,24 @@ void orc_weights_inv_dist_sq(const double* dist, size_t N, double* w_out);
 int orc_weighted_cov_cholesky(const double* theta, const double* w, size_t N, size_t P,
                               double scale, double* cov, double* chol);
 
+/* CPU baseline: the Julia forward model (src/cpu/simulate.jl) in Float64,
+ * timed over many proposals on nthreads host threads (cpu_baseline.c). */
+typedef struct orc_cpu_job {
+    uint32_t C;
+    int32_t lognormal;
+    double m[ORC_MAX_COMPONENTS]; /* discrete: D [um^2/s]; lognormal: mean diameter [nm] */
+    double s[ORC_MAX_COMPONENTS]; /* lognormal: diameter sd [nm] */
+    double c[ORC_MAX_COMPONENTS]; /* concentration [particles/ml] */
+    double az[ORC_MAX_COMPONENTS];
+    double temperature, viscosity;
+    double ax, ay, Lx, Ly, Lz, deltat, ub_de;
+    uint32_t kmin, B, V;
+    const uint32_t* frames;
+} orc_cpu_job;
+
+uint64_t orc_cpu_forward_batch(const orc_cpu_job* jobs, uint32_t n_jobs, uint32_t nthreads,
+                               uint64_t seed, double* seconds, uint64_t* checksum);
+
 #ifdef __cplusplus
 }
 #endif

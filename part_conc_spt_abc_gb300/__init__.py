@@ -79,6 +79,23 @@ class Context:
             setattr(t, k, v)
         check(lib().pcs_set_tuning(self.h, C.byref(t)), "pcs_set_tuning")
 
+    def timer_start(self) -> None:
+        check(lib().pcs_timer_start(self.h), "pcs_timer_start")
+
+    def timer_stop(self) -> float:
+        """Milliseconds on the context's stream since timer_start()."""
+        ms = C.c_double(0)
+        check(lib().pcs_timer_stop(self.h, C.byref(ms)), "pcs_timer_stop")
+        return ms.value
+
+    def kernel_stats(self) -> _lib.KernelStats:
+        s = _lib.KernelStats()
+        check(lib().pcs_get_kernel_stats(self.h, C.byref(s)), "pcs_get_kernel_stats")
+        return s
+
+    def reset_kernel_stats(self) -> None:
+        check(lib().pcs_reset_kernel_stats(self.h), "pcs_reset_kernel_stats")
+
     def autotune(self, inp: "Input") -> _lib.Tuning:
         t = _lib.Tuning()
         obs, keep = inp.observed()

@@ -72,6 +72,15 @@ class JobInfo(C.Structure):
     ]
 
 
+class KernelStats(C.Structure):
+    _fields_ = [
+        ("rounds", C.c_uint64), ("kernel_launches", C.c_uint64), ("simulate_launches", C.c_uint64),
+        ("simulate_ms", C.c_double), ("distance_launches", C.c_uint64), ("distance_ms", C.c_double),
+        ("round_ms", C.c_double), ("proposals", C.c_uint64), ("particle_steps", C.c_uint64),
+        ("histogram_cells", C.c_uint64),
+    ]
+
+
 class Setup(C.Structure):
     _fields_ = [
         ("model", C.c_int32), ("component_count", C.c_uint32), ("video_count", C.c_uint32),
@@ -120,6 +129,10 @@ SIGNATURES = {
     "pcs_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "pcs_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "pcs_autotune": (C.c_int, [C.c_void_p, C.POINTER(Params), C.POINTER(Observed), C.POINTER(Tuning)]),
+    "pcs_timer_start": (C.c_int, [C.c_void_p]),
+    "pcs_timer_stop": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "pcs_get_kernel_stats": (C.c_int, [C.c_void_p, C.POINTER(KernelStats)]),
+    "pcs_reset_kernel_stats": (C.c_int, [C.c_void_p]),
     "pcs_job_create": (C.c_int, [C.c_void_p, C.POINTER(Params), C.POINTER(Observed), C.c_uint64, C.POINTER(C.c_void_p)]),
     "pcs_job_destroy": (C.c_int, [C.c_void_p]),
     "pcs_job_run": (C.c_int, [C.c_void_p, C.c_uint32]),

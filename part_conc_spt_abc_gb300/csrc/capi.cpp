@@ -235,6 +235,44 @@ pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t)
     });
 }
 
+pcs_status pcs_timer_start(pcs_ctx* ctx)
+{
+    return guard([&] {
+        Ctx& c = C_(ctx);
+        PCS_CUDA(cudaEventRecord(c.ev_t0, c.stream));
+    });
+}
+
+pcs_status pcs_timer_stop(pcs_ctx* ctx, double* elapsed_ms)
+{
+    return guard([&] {
+        Ctx& c = C_(ctx);
+        need(elapsed_ms, "elapsed_ms");
+        PCS_CUDA(cudaEventRecord(c.ev_t1, c.stream));
+        PCS_CUDA(cudaEventSynchronize(c.ev_t1));
+        float ms = 0;
+        PCS_CUDA(cudaEventElapsedTime(&ms, c.ev_t0, c.ev_t1));
+        *elapsed_ms = ms;
+    });
+}
+
+pcs_status pcs_get_kernel_stats(pcs_ctx* ctx, pcs_kernel_stats* out)
+{
+    return guard([&] {
+        Ctx& c = C_(ctx);
+        need(out, "out");
+        *out = c.stats;
+    });
+}
+
+pcs_status pcs_reset_kernel_stats(pcs_ctx* ctx)
+{
+    return guard([&] {
+        Ctx& c = C_(ctx);
+        std::memset(&c.stats, 0, sizeof c.stats);
+    });
+}
+
 /* ----------------------------------------------------------------------- */
 /* jobs                                                                    */
 /* ----------------------------------------------------------------------- */

@@ -413,6 +413,9 @@ Ctx::Ctx(int dev, int infl) : device(dev), inflight(infl > 0 ? infl : 1)
     *h_err = 0;
     PCS_CUDA(cudaEventCreate(&ev0));
     PCS_CUDA(cudaEventCreate(&ev1));
+    for (cudaEvent_t* e : {&ev_sim0, &ev_sim1, &ev_dist0, &ev_dist1, &ev_t0, &ev_t1}) PCS_CUDA(cudaEventCreate(e));
+    PCS_CUDA(cudaMallocHost((void**)&h_round_out, sizeof(RoundDev)));
+    std::memset(h_round_out, 0, sizeof(RoundDev));
 }
 
 Ctx::~Ctx()
@@ -425,6 +428,9 @@ Ctx::~Ctx()
     if (h_round) cudaFreeHost(h_round);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    for (cudaEvent_t e : {ev_sim0, ev_sim1, ev_dist0, ev_dist1, ev_t0, ev_t1})
+        if (e) cudaEventDestroy(e);
+    if (h_round_out) cudaFreeHost(h_round_out);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -553,7 +559,9 @@ void Ctx::enqueue_round()
     l.replay = false;
     l.aggregate = tune.aggregate == 1u;
     l.grid = sim_grid(l.block, tune.ppt, l.aggregate, s.tile_words);
+    PCS_CUDA(cudaEventRecord(ev_sim0, stream));
     PCS_CUDA(launch_simulate(s, l, stream));
+    PCS_CUDA(cudaEventRecord(ev_sim1, stream));
 
     DistArgs d{};
     d.jobs = a.jobs;
@@ -566,12 +574,15 @@ void Ctx::enqueue_round()
     d.ssd = nullptr;
     d.err = a.err;
     d.max_rows = rb.max_rows;
+    PCS_CUDA(cudaEventRecord(ev_dist0, stream));
     PCS_CUDA(launch_distance(d, std::min<uint32_t>(rb.capacity, 2u * (uint32_t)sm_count), stream));
+    PCS_CUDA(cudaEventRecord(ev_dist1, stream));
 
     PCS_CUDA(launch_accept(a, kMaxRoundJobs, stream));
     PCS_CUDA(launch_finalize(a, kMaxRoundJobs, rb.max_n, stream));
     PCS_CUDA(cudaMemcpyAsync(h_status, rb.pmc.p, sizeof(JobPmcDev) * kMaxRoundJobs, cudaMemcpyDeviceToHost, stream));
     PCS_CUDA(cudaMemcpyAsync(h_err, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    PCS_CUDA(cudaMemcpyAsync(h_round_out, rb.round.p, sizeof(RoundDev), cudaMemcpyDeviceToHost, stream));
 }
 
 void Ctx::run_round(double* ms_out)
@@ -604,9 +615,21 @@ void Ctx::run_round(double* ms_out)
     }
     PCS_CUDA(cudaEventRecord(ev1, stream));
     PCS_CUDA(cudaStreamSynchronize(stream));
-    float ms = 0.0f;
+    float ms = 0.0f, sim_ms = 0.0f, dist_ms = 0.0f;
     PCS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    PCS_CUDA(cudaEventElapsedTime(&sim_ms, ev_sim0, ev_sim1));
+    PCS_CUDA(cudaEventElapsedTime(&dist_ms, ev_dist0, ev_dist1));
     if (ms_out) *ms_out = ms;
+    stats.rounds += 1;
+    stats.kernel_launches += kKernelsPerRound;
+    stats.simulate_launches += 1;
+    stats.simulate_ms += sim_ms;
+    stats.distance_launches += 1;
+    stats.distance_ms += dist_ms;
+    stats.round_ms += ms;
+    stats.proposals += h_round_out->n_props;
+    stats.particle_steps += h_round_out->round_steps;
+    stats.histogram_cells += h_round_out->round_cells;
     if (*h_err) {
         const uint32_t bits = *h_err;
         *h_err = 0;

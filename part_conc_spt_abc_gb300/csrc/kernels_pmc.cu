@@ -192,12 +192,14 @@ __global__ void k_round_plan(PmcArgs a)
     rd->n_props = base;
     rd->n_items = 0u;
     rd->queue_head = 0u;
+    rd->round_steps = 0ull;
+    rd->round_cells = hbase;
 }
 
 /* ----------------------------------------------------------------------- */
 __global__ void __launch_bounds__(128) k_propose(PmcArgs a)
 {
-    const RoundDev* rd = a.round;
+    RoundDev* rd = a.round;
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= rd->n_props) return;
     const uint32_t j = job_of_(rd, q);
@@ -323,6 +325,7 @@ __global__ void __launch_bounds__(128) k_propose(PmcArgs a)
     pd.item_begin = 0u;
     a.props[q] = pd;
     atomicAdd((unsigned long long*)&pm.particle_steps, (unsigned long long)steps);
+    atomicAdd(&a.round->round_steps, (unsigned long long)steps);
 }
 
 /* ----------------------------------------------------------------------- */

@@ -123,6 +123,8 @@ struct RoundDev {
     uint32_t n_items;
     uint32_t queue_head;
     uint32_t pad;
+    unsigned long long round_steps;  /* particle-steps of the round's proposals */
+    unsigned long long round_cells;  /* histogram cells of the round's proposals */
     uint32_t job_base[64];    /* first proposal of each job */
     uint32_t job_k[64];       /* trials per pending slot */
     uint32_t job_count[64];   /* proposals of each job */
