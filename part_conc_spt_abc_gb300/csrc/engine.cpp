@@ -559,9 +559,9 @@ void Ctx::enqueue_round()
     l.replay = false;
     l.aggregate = tune.aggregate == 1u;
     l.grid = sim_grid(l.block, tune.ppt, l.aggregate, s.tile_words);
-    PCS_CUDA(cudaEventRecord(ev_sim0, stream));
+    PCS_CUDA(cudaEventRecordWithFlags(ev_sim0, stream, cudaEventRecordExternal));
     PCS_CUDA(launch_simulate(s, l, stream));
-    PCS_CUDA(cudaEventRecord(ev_sim1, stream));
+    PCS_CUDA(cudaEventRecordWithFlags(ev_sim1, stream, cudaEventRecordExternal));
 
     DistArgs d{};
     d.jobs = a.jobs;
@@ -574,9 +574,9 @@ void Ctx::enqueue_round()
     d.ssd = nullptr;
     d.err = a.err;
     d.max_rows = rb.max_rows;
-    PCS_CUDA(cudaEventRecord(ev_dist0, stream));
+    PCS_CUDA(cudaEventRecordWithFlags(ev_dist0, stream, cudaEventRecordExternal));
     PCS_CUDA(launch_distance(d, std::min<uint32_t>(rb.capacity, 2u * (uint32_t)sm_count), stream));
-    PCS_CUDA(cudaEventRecord(ev_dist1, stream));
+    PCS_CUDA(cudaEventRecordWithFlags(ev_dist1, stream, cudaEventRecordExternal));
 
     PCS_CUDA(launch_accept(a, kMaxRoundJobs, stream));
     PCS_CUDA(launch_finalize(a, kMaxRoundJobs, rb.max_n, stream));
