@@ -318,6 +318,29 @@ pcs_status pcs_scan_distance(pcs_ctx* ctx, const uint32_t* hist, const uint32_t*
                              uint32_t rows, uint32_t bins, uint32_t count, uint32_t* cum_out,
                              float* dist_f32, double* dist_f64, uint64_t* ssd);
 
+/* pcs_scan_distance for callers that cannot allocate device memory; this
+ * entry point has no counterpart in the reference.  Callers capturing a CUDA
+ * graph, hosts whose own caching allocator owns all device memory, and
+ * real-time loops where an allocation could stall on device synchronisation
+ * cannot let a library call cudaMalloc; this variant takes device pointers
+ * and keeps its working buffers (the transposed observed histogram and one
+ * descriptor per histogram) in a fixed __device__ array instead, calling no
+ * allocator.  d_hist holds count x rows x bins counts and is reset to zero,
+ * as K_distance resets its input; d_ref_sat is rows x bins; d_dist_f32 gets
+ * count float distances in the reference kernel's reduction order.  Work is
+ * queued on `stream` (a cudaStream_t, NULL = default stream) of the current
+ * device; the call does not wait for it.  Limits: rows * bins <=
+ * PCS_NOALLOC_MAX_CELLS and count <= PCS_NOALLOC_MAX_COUNT, else
+ * PCS_ERR_INVALID_ARGUMENT.  The array (about 4.7 MiB) stays reserved on each
+ * GPU that loads the library until exit.  The first call on a device looks
+ * the array's address up (cudaGetSymbolAddress), so make it before any stream
+ * capture.  All calls share the array: calls whose work overlaps on the GPU
+ * race and must not be issued. */
+#define PCS_NOALLOC_MAX_CELLS 1048576u
+#define PCS_NOALLOC_MAX_COUNT 4096u
+pcs_status pcs_scan_distance_noalloc(uint32_t* d_hist, const uint32_t* d_ref_sat, uint32_t rows,
+                                     uint32_t bins, uint32_t count, float* d_dist_f32, void* stream);
+
 /* Observed cumulative histogram from K / DE lists, on the device. */
 pcs_status pcs_observed_sat(pcs_ctx* ctx, const uint32_t* K, const double* DE, size_t n,
                             uint32_t rows, uint32_t bins, double ub_de, uint32_t* sat_out);
