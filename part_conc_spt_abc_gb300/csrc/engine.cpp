@@ -575,7 +575,7 @@ void Ctx::enqueue_round()
     d.err = a.err;
     d.max_rows = rb.max_rows;
     PCS_CUDA(cudaEventRecordWithFlags(ev_dist0, stream, cudaEventRecordExternal));
-    PCS_CUDA(launch_distance(d, std::min<uint32_t>(rb.capacity, 2u * (uint32_t)sm_count), stream));
+    PCS_CUDA(launch_distance(d, std::min<uint32_t>(rb.capacity, (uint32_t)(distance_ctas_per_sm(rb.max_rows) * sm_count)), stream));
     PCS_CUDA(cudaEventRecordWithFlags(ev_dist1, stream, cudaEventRecordExternal));
 
     PCS_CUDA(launch_accept(a, kMaxRoundJobs, stream));

@@ -56,7 +56,7 @@ struct Tuning {
     uint32_t aggregate = 0;
     uint32_t chunk = 1024;
     uint32_t capacity = 2048;
-    uint32_t max_spec = 16;
+    uint32_t max_spec = 4096;
     uint32_t use_graphs = 1;
 };
 

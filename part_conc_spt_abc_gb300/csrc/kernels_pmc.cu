@@ -172,7 +172,17 @@ __global__ void k_round_plan(PmcArgs a)
     uint64_t hbase = 0;
     for (uint32_t j = 0; j < rd->n_jobs; ++j) {
         const JobPmcDev& pm = a.pmc[j];
-        uint32_t kj = (pm.generation == 0u) ? 1u : k; /* prior pass: one simulation per slot */
+        /* trials per pending slot: enough to fill the round, but not many
+         * more than ~0.3 / (acceptance rate so far), so that few trials
+         * are simulated after a slot's first acceptance */
+        uint32_t kj = k;
+        if (pm.generation == 0u) {
+            kj = 1u; /* prior pass: one simulation per slot */
+        } else {
+            const double pacc = ((double)pm.accepted_gen + 1.0) / ((double)pm.trials + 2.0);
+            const double kw = ceil(0.3 / pacc);
+            if (kw < (double)kj) kj = (uint32_t)(kw < 1.0 ? 1.0 : kw);
+        }
         uint64_t want = pm.done ? 0u : (uint64_t)pm.pending_count * kj;
         uint64_t room = rd->capacity - base;
         const uint64_t rb = (uint64_t)a.jobs[j].R * a.jobs[j].B;
@@ -370,7 +380,7 @@ __global__ void __launch_bounds__(1024) k_items(PmcArgs a)
 /* accept: one block per job */
 __global__ void __launch_bounds__(1024) k_accept(PmcArgs a)
 {
-    __shared__ uint32_t s_keep;
+    __shared__ uint32_t s_keep, s_exhausted;
     __shared__ unsigned long long s_trials, s_acc;
     const uint32_t j = blockIdx.x;
     RoundDev* rd = a.round;
@@ -385,6 +395,7 @@ __global__ void __launch_bounds__(1024) k_accept(PmcArgs a)
     const uint32_t P = pm.P;
     if (threadIdx.x == 0) {
         s_keep = 0u;
+        s_exhausted = 0u;
         s_trials = 0ull;
         s_acc = 0ull;
         pm.gen_ended = 0u;
@@ -420,6 +431,10 @@ __global__ void __launch_bounds__(1024) k_accept(PmcArgs a)
             } else {
                 pm.next_trial[slot] += k;
                 atomicAdd(&s_trials, (unsigned long long)k);
+                /* the trial ordinal has 20 bits in the random-stream counter:
+                 * a slot that exhausts them ends the generation like the
+                 * trial cap does (converged) */
+                if (pm.next_trial[slot] + rd->max_spec >= (1u << 20)) s_exhausted = 1u;
             }
         }
         if (!acc_ok) keep_list[atomicAdd(&s_keep, 1u)] = slot;
@@ -432,6 +447,8 @@ __global__ void __launch_bounds__(1024) k_accept(PmcArgs a)
         pm.trials += s_trials;
         pm.simulations += cnt;
         pm.accepted_total += s_acc;
+        pm.accepted_gen += s_acc;
+        if (s_exhausted && pm.generation > 0u) pm.trials = (uint64_t)pm.avg_trials * pm.N;
         const bool cap = pm.generation > 0u &&
                          (double)pm.trials >= (double)pm.avg_trials * (double)pm.N;
         if (nk == 0u || cap) pm.gen_ended = 1u;
@@ -589,6 +606,7 @@ __device__ void start_generation_(JobPmcDev& pm)
     pm.generation += 1u;
     pm.pending_count = pm.N;
     pm.trials = 0ull;
+    pm.accepted_gen = 0ull;
     pm.gen_ended = 0u;
 }
 

@@ -161,7 +161,8 @@ extern "C" pcs_status pcs_scan_distance_noalloc(uint32_t* d_hist, const uint32_t
     d.max_rows = rows;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const uint32_t grid = count < 2u * (uint32_t)sms ? count : 2u * (uint32_t)sms;
+    const uint32_t cap = (uint32_t)(pcs::distance_ctas_per_sm(rows) * sms);
+    const uint32_t grid = count < cap ? count : cap;
     e = pcs::launch_distance(d, grid ? grid : 1u, st);
     if (e != cudaSuccess) return fail_(PCS_ERR_CUDA, std::string("distance launch: ") + cudaGetErrorString(e));
     return fail_(PCS_OK, "");

@@ -66,6 +66,8 @@ struct DistArgs {
 };
 cudaError_t launch_distance(const DistArgs& a, uint32_t grid, cudaStream_t st);
 size_t distance_smem_bytes(uint32_t max_rows);
+uint32_t distance_block_threads(uint32_t max_rows);
+int distance_ctas_per_sm(uint32_t max_rows);
 const uint32_t kDistRowBlock = 256;
 
 /* ---------------- ABC-PMC step (kernels_pmc.cu) ---------------- */
@@ -99,6 +101,7 @@ struct JobPmcDev {
     uint64_t trials;      /* semantic trials of the running generation */
     uint64_t simulations; /* all proposals simulated */
     uint64_t accepted_total;
+    uint64_t accepted_gen;    /* accepted in the running generation */
     uint64_t particle_steps;
     uint32_t iterations;  /* reference "iterations" counter */
     uint32_t converged;

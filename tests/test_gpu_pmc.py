@@ -1,0 +1,162 @@
+"""The ABC-PMC engine on the GPU: invariants of every generation, results
+independent of how work is batched (round capacity, speculation, launch
+shape, other jobs sharing the rounds), the accel drop-in end to end."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def small_input(pcs, seed=0, C=1, schedule=None, weighting=0, model=None, videos=6, frames=60, pop=96):
+    import part_conc_spt_abc_gb300.workloads as W
+    ctx = pcs.Context(0)
+    try:
+        mu = [175.0, 500.0][:C]
+        sd = [10.0, 25.0][:C]
+        w = [0.6, 0.4][:C]
+        inp, truth = W.make_problem(ctx, mu, sd, 3e14, w, videos, frames, 48, pop, 4, seed=seed)
+    finally:
+        ctx.close()
+    p = inp.params
+    p.avg_trial_count = 200
+    p.weighting_scheme = weighting
+    if schedule is not None:
+        p.schedule = schedule
+    return inp, truth
+
+
+def run_job(pcs, ctx, inp, seed, steps):
+    sim = pcs.make_simulation(ctx, inp, seed)
+    for _ in range(steps):
+        if sim.step():
+            break
+    out = sim.output()
+    info = sim.info()
+    sim.close()
+    return out, info
+
+
+def test_generation_invariants(pcs, ctx):
+    inp, truth = small_input(pcs, C=2)
+    sim = pcs.make_simulation(ctx, inp, 5)
+    p = inp.params
+    for g in range(4):
+        done = sim.step()
+        out = sim.output()
+        info = sim.info()
+        N = p.abc_sample_count
+        assert out.w.shape == (N,) and abs(out.w.sum() - 1.0) < 1e-9 and (out.w > 0).all()
+        m = out.m.reshape(N, 2)
+        assert (np.diff(m, axis=1) >= 0).all(), "components sorted by mean diameter"
+        assert (m >= p.lb_m).all() and (m <= p.ub_m).all()
+        c = np.log10(out.c)
+        assert (c >= np.log10(p.lb_c) - 1e-9).all() and (c <= np.log10(p.ub_c) + 1e-9).all()
+        assert (out.az == 2.0).all(), "a parameter with equal bounds stays fixed"
+        if g >= 1:
+            assert np.isfinite(out.dist).all()
+        if done:
+            break
+    assert info.iterations >= 2 and info.simulations > 0 and info.particle_steps > 0
+
+
+def test_results_do_not_depend_on_batching(pcs, ctx):
+    inp, _ = small_input(pcs, C=1, pop=64)
+    ref_out, ref_info = run_job(pcs, ctx, inp, 9, 3)
+    settings = [dict(max_speculation=1), dict(max_speculation=3, block_size=128, particles_per_thread=2),
+                dict(round_capacity=200, max_speculation=64),
+                dict(max_speculation=4096, block_size=512, particles_per_thread=4, hist_tile_rows=8,
+                     warp_aggregate=1)]
+    try:
+        for kw in settings:
+            ctx.set_tuning(**kw)
+            out, info = run_job(pcs, ctx, inp, 9, 3)
+            for f in ["m", "c", "az", "dist", "w", "s"]:
+                assert np.array_equal(getattr(out, f), getattr(ref_out, f)), (kw, f)
+            assert info.trials == ref_info.trials and info.accepted == ref_info.accepted
+            assert info.gamma == ref_info.gamma
+    finally:
+        ctx.set_tuning(max_speculation=4096, block_size=256, particles_per_thread=1, hist_tile_rows=64,
+                       warp_aggregate=0xFFFFFFFF, round_capacity=2048)
+
+
+def test_serve_alone_equals_mix(pcs, ctx):
+    jobs = [small_input(pcs, seed=s, C=1 + s % 2, pop=48 + 16 * s)[0] for s in range(3)]
+    alone = []
+    for i, inp in enumerate(jobs):
+        out, _ = run_job(pcs, ctx, inp, 100 + i, 1000)
+        alone.append(out)
+    srv = pcs.Server(ctx)
+    sims = [pcs.make_simulation(ctx, inp, 100 + i) for i, inp in enumerate(jobs)]
+    for s in sims:
+        srv.submit(s)
+    for _ in range(100000):
+        if srv.step() == 0:
+            break
+    for s, a in zip(sims, alone):
+        assert srv.finished(s)
+        b = s.output()
+        for f in ["m", "c", "az", "dist", "w"]:
+            assert np.array_equal(getattr(a, f), getattr(b, f)), f
+        s.close()
+
+
+def test_inverse_distance_weights(pcs, ctx):
+    inp, _ = small_input(pcs, C=1, weighting=1)
+    out, info = run_job(pcs, ctx, inp, 3, 3)
+    w = 1.0 / out.dist ** 2
+    np.testing.assert_allclose(out.w, w / w.sum(), rtol=1e-12)
+
+
+def test_max_steps_semantics(pcs, ctx):
+    """-S n stops when the iteration counter exceeds n (the counter then
+    reads n + 1, as the reference's meta does)."""
+    inp, _ = small_input(pcs, C=1, pop=32)
+    inp.params.max_generations = 0
+    sim = pcs.make_simulation(ctx, inp, 1)
+    sim.run(2)
+    info = sim.info()
+    assert info.iterations == 3 and not info.converged
+    sim.close()
+
+
+def test_accel_end_to_end(pcs, ctx, tmp_path):
+    inp, _ = small_input(pcs, C=2, pop=48)
+    p = inp.params
+    data = tmp_path / "data.xml"
+    data.write_text("<data>\n\t<ax>%r</ax>\n\t<ay>%r</ay>\n\t<number_of_frames>%s</number_of_frames>\n\t<deltat>%r</deltat>\n"
+                    "\t<K>%s</K>\n\t<DE>%s</DE>\n</data>" % (
+                        inp.ax, inp.ay, ",".join(str(int(x)) for x in inp.frames), inp.deltat,
+                        ",".join(str(int(x)) for x in inp.K), ",".join(repr(float(x)) for x in inp.DE)))
+    xml = tmp_path / "input.xml"
+    tags = dict(data_file_path=str(data), model="lognormal", number_of_components=2, weighting_scheme="pmc-standard",
+                Lx=p.Lx, Ly=p.Ly, Lz=p.Lz, kmin=2, number_of_de_bins=p.de_bin_count, ub_de=p.ub_de, lb_m=p.lb_m,
+                ub_m=p.ub_m, lb_s=p.lb_s, ub_s=p.ub_s, lb_c=p.lb_c, ub_c=p.ub_c, lb_az=p.lb_az, ub_az=p.ub_az,
+                number_of_abc_samples=48, gamma_initial=15.0, gamma_adaptive="true", delta_gamma=0.05,
+                ub_average_number_of_trials=50, output_file_path=str(tmp_path / "never.xml"))
+    xml.write_text("<input>\n" + "".join(f"\t<{k}>{v}</{k}>\n" for k, v in tags.items()) + "</input>\n")
+    out = tmp_path / "out.xml"
+    r = subprocess.run([pcs._lib.ACCEL_PATH, "-i", str(xml), "-o", str(out), "-S", "2", "-F", "7", "-q"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    o = pcs.load_output(str(out))
+    assert o.model == 2 and o.abc_sample_count == 48 and o.component_count == 2
+    assert len(o.m) == 96 and len(o.s) == 96 and len(o.w) == 48
+    meta = dict(o.meta)
+    assert meta["iterations"] == "3" and meta["simulator"] == "gpu" and meta["gpu0_queues"] == "30"
+    # same seed, same result
+    out2 = tmp_path / "out2.xml"
+    r = subprocess.run([pcs._lib.ACCEL_PATH, "-i", str(xml), "-o", str(out2), "-S", "2", "-F", "7", "-q"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0
+    o2 = pcs.load_output(str(out2))
+    assert np.array_equal(o.m, o2.m) and np.array_equal(o.w, o2.w)
+
+
+def test_autotune(pcs, ctx):
+    inp, _ = small_input(pcs, C=1, pop=64)
+    t = ctx.autotune(inp)
+    assert t.block_size in (128, 256, 512, 1024) and t.particles_per_thread in (1, 2, 4)
+    ctx.set_tuning(block_size=256, particles_per_thread=1, hist_tile_rows=64, warp_aggregate=0xFFFFFFFF)
