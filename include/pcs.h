@@ -179,6 +179,11 @@ pcs_status pcs_job_destroy(pcs_job* job);
 /* Runs to convergence, or for max_steps generations when max_steps > 0
  * (accel -S).  Blocking; one job at a time (the plain form). */
 pcs_status pcs_job_run(pcs_job* job, uint32_t max_steps);
+/* The plain form: the reference's schedule (host-side PMC in double, one
+ * proposal per simulate + distance launch, `queues` streams in flight, at most
+ * one trial per population slot in flight; src/gpu/detail/simulation_impl.inl
+ * :178-455) on this build's kernels.  For comparison with pcs_job_run. */
+pcs_status pcs_job_run_plain(pcs_job* job, uint32_t max_steps, uint32_t queues);
 /* Advances a job by one generation (batched rounds until every slot is
  * accepted or the trial cap is hit).  *done becomes 1 when it has finished. */
 pcs_status pcs_job_step(pcs_job* job, int* done);

@@ -214,6 +214,10 @@ class Simulation:
     def run(self, max_steps: int = 0) -> None:
         check(lib().pcs_job_run(self.h, max_steps), "Simulation::run")
 
+    def run_plain(self, max_steps: int = 0, queues: int = 30) -> None:
+        """The reference's one-proposal-per-launch schedule on these kernels."""
+        check(lib().pcs_job_run_plain(self.h, max_steps, queues), "pcs_job_run_plain")
+
     def step(self) -> bool:
         done = C.c_int(0)
         check(lib().pcs_job_step(self.h, C.byref(done)), "pcs_job_step")

@@ -136,6 +136,7 @@ SIGNATURES = {
     "pcs_job_create": (C.c_int, [C.c_void_p, C.POINTER(Params), C.POINTER(Observed), C.c_uint64, C.POINTER(C.c_void_p)]),
     "pcs_job_destroy": (C.c_int, [C.c_void_p]),
     "pcs_job_run": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "pcs_job_run_plain": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "pcs_job_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "pcs_job_info_get": (C.c_int, [C.c_void_p, C.POINTER(JobInfo)]),
     "pcs_job_output": (C.c_int, [C.c_void_p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p]),

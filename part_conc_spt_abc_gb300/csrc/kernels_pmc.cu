@@ -35,95 +35,11 @@
 
 #include "pcs_common.h"
 #include "pcs_kernels.h"
+#include "pcs_proposal.h"
 
 namespace pcs {
 
 namespace {
-
-__device__ __forceinline__ double u53_(pcs_u4 r, int half)
-{
-    return half ? pcs_u01_53(r.z, r.w) : pcs_u01_53(r.x, r.y);
-}
-
-/* standard normal pair from 4 words (Box-Muller, double) */
-__device__ __forceinline__ void normal2_(pcs_u4 r, double& n0, double& n1)
-{
-    double u1 = 1.0 - pcs_u01_53(r.x, r.y); /* (0, 1] */
-    double u2 = pcs_u01_53(r.z, r.w);
-    double rad = sqrt(-2.0 * log(u1));
-    double s, c;
-    sincospi(2.0 * u2, &s, &c);
-    n0 = rad * s;
-    n1 = rad * c;
-}
-
-/* displace_ reflection (simulation_impl.inl:72-76), with a bounded loop */
-__device__ double reflect_(double bis, double lo, double hi)
-{
-    for (int it = 0; it < 64 && (bis < lo || bis > hi); ++it) {
-        if (bis < lo) bis += 2.0 * (lo - bis);
-        if (bis > hi) bis -= 2.0 * (bis - hi);
-    }
-    if (bis < lo || bis > hi) {
-        /* far outside: fold with the period of the reflection */
-        double w = hi - lo;
-        double t = fmod(fabs(bis - lo), 2.0 * w);
-        bis = lo + (t <= w ? t : 2.0 * w - t);
-    }
-    return bis;
-}
-
-/* Poisson(lambda): inversion for small means, PTRS transformed rejection
- * (W. Hoermann, "The transformed rejection method for generating Poisson
- * random variables", Insurance: Mathematics and Economics 12, 1993). */
-__device__ uint32_t poisson_(double lam, uint32_t video, uint32_t slot, uint32_t gt, uint32_t k0,
-                             uint32_t k1)
-{
-    if (!(lam > 0.0)) return 0u;
-    if (lam < 12.0) {
-        pcs_u4 r = pcs_philox(video, pcs_ctr_tag(PCS_STREAM_POISSON, 0u), slot, gt, k0, k1);
-        double u = pcs_u01_53(r.x, r.y);
-        double p = exp(-lam), F = p;
-        uint32_t k = 0;
-        while (u > F && k < 1000u) {
-            ++k;
-            p *= lam / k;
-            F += p;
-        }
-        return k;
-    }
-    const double slam = sqrt(lam), loglam = log(lam);
-    const double b = 0.931 + 2.53 * slam;
-    const double a = -0.059 + 0.02483 * b;
-    const double invalpha = 1.1239 + 1.1328 / (b - 3.4);
-    const double vr = 0.9277 - 3.6224 / (b - 2.0);
-    for (uint32_t it = 0; it < 256u; ++it) {
-        pcs_u4 r = pcs_philox(video, pcs_ctr_tag(PCS_STREAM_POISSON, 1u + it), slot, gt, k0, k1);
-        double U = pcs_u01_53(r.x, r.y) - 0.5;
-        double V = pcs_u01_53(r.z, r.w);
-        double us = 0.5 - fabs(U);
-        double kf = floor((2.0 * a / us + b) * U + lam + 0.43);
-        if (us >= 0.07 && V <= vr) return (uint32_t)kf;
-        if (kf < 0.0 || (us < 0.013 && V > us)) continue;
-        if (log(V) + log(invalpha) - log(a / (us * us) + b) <= -lam + kf * loglam - lgamma(kf + 1.0))
-            return (uint32_t)kf;
-    }
-    return (uint32_t)floor(lam + 0.5);
-}
-
-/* index of the first cumulative weight >= u (std::lower_bound), clamped */
-__device__ uint32_t pick_(const double* wcum, uint32_t N, double u)
-{
-    uint32_t lo = 0, hi = N;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (wcum[mid] < u)
-            lo = mid + 1;
-        else
-            hi = mid;
-    }
-    return lo < N ? lo : N - 1;
-}
 
 __device__ uint32_t job_of_(const RoundDev* rd, uint32_t q)
 {
@@ -134,23 +50,6 @@ __device__ uint32_t job_of_(const RoundDev* rd, uint32_t q)
     for (uint32_t i = 0; i < rd->n_jobs; ++i)
         if (q >= rd->job_base[i] && q < rd->job_base[i] + rd->job_count[i]) return i;
     return j;
-}
-
-/* parameter layout: [m | s (lognormal) | log10c | az] */
-struct Layout {
-    uint32_t m, s, c, az, C, Z;
-};
-
-__device__ __forceinline__ Layout layout_(const JobPmcDev& pm)
-{
-    Layout L;
-    L.C = pm.C;
-    L.Z = pm.Z;
-    L.m = 0;
-    L.s = pm.C;
-    L.c = (pm.model == PCS_DEV_MODEL_LOGNORMAL) ? 2 * pm.C : pm.C;
-    L.az = L.c + pm.C;
-    return L;
 }
 
 } // namespace
@@ -221,112 +120,25 @@ __global__ void __launch_bounds__(128) k_propose(PmcArgs a)
     const uint32_t slot = pm.pending[pend_idx];
     const uint32_t trial = pm.next_trial[slot] + rep;
     const uint32_t gen = pm.generation;
-    const uint32_t gt = pcs_ctr_gen_trial(gen, trial);
     const uint32_t k0 = jd.seed_lo, k1 = jd.seed_hi;
-    const uint32_t P = pm.P, N = pm.N;
-    const Layout L = layout_(pm);
 
     double th[PCS_MAX_P];
-    if (gen == 0u) {
-        for (uint32_t p = 0; p < P; ++p) th[p] = pm.theta[(uint64_t)slot * P + p];
-    } else {
-        pcs_u4 r = pcs_philox(0u, pcs_ctr_tag(PCS_STREAM_PICK, 0u), slot, gt, k0, k1);
-        const uint32_t parent = pick_(pm.wcum, N, u53_(r, 0));
-        const double* tp = pm.theta + (uint64_t)parent * P;
-        double nrm[PCS_MAX_P];
-        for (uint32_t p = 0; p < P; p += 2) {
-            pcs_u4 rr = pcs_philox(p >> 1, pcs_ctr_tag(PCS_STREAM_PERTURB, 0u), slot, gt, k0, k1);
-            double n0, n1;
-            normal2_(rr, n0, n1);
-            nrm[p] = n0;
-            if (p + 1 < P) nrm[p + 1] = n1;
-        }
-        for (uint32_t p = 0; p < P; ++p) {
-            if (pm.fixed[p]) {
-                th[p] = pm.lo[p];
-                continue;
-            }
-            double delta;
-            if (pm.perturbation == 1u) {
-                delta = 0.0;
-                for (uint32_t i = 0; i <= p; ++i)
-                    if (!pm.fixed[i]) delta += pm.factor[p * P + i] * nrm[i];
-            } else {
-                delta = pm.factor[p * P + p] * nrm[p];
-            }
-            th[p] = reflect_(tp[p] + delta, pm.lo[p], pm.hi[p]);
-        }
-        /* sort components by the first parameter group (label switching) */
-        for (uint32_t i = 1; i < L.C; ++i) {
-            for (uint32_t x = i; x > 0 && th[L.m + x] < th[L.m + x - 1]; --x) {
-                double t;
-                t = th[L.m + x]; th[L.m + x] = th[L.m + x - 1]; th[L.m + x - 1] = t;
-                t = th[L.c + x]; th[L.c + x] = th[L.c + x - 1]; th[L.c + x - 1] = t;
-                if (pm.model == PCS_DEV_MODEL_LOGNORMAL) {
-                    t = th[L.s + x]; th[L.s + x] = th[L.s + x - 1]; th[L.s + x - 1] = t;
-                }
-                if (L.Z > 1u) {
-                    t = th[L.az + x]; th[L.az + x] = th[L.az + x - 1]; th[L.az + x - 1] = t;
-                }
-            }
-        }
-    }
+    pcs_build_theta(pm, pm.theta, pm.wcum, pm.factor, slot, trial, gen, k0, k1, th);
     double* out = a.theta_prop + (uint64_t)q * PCS_MAX_P;
-    for (uint32_t p = 0; p < P; ++p) out[p] = th[p];
+    for (uint32_t p = 0; p < pm.P; ++p) out[p] = th[p];
 
-    /* forward-model arguments (simulation_impl.inl:293-340) */
     PropDev pd;
     pd.job = j;
     pd.slot = slot;
     pd.trial = trial;
     pd.gen = gen;
     pd.quirk_full_az = 0u;
-    double powc[PCS_MAX_C], csum = 0.0;
-    for (uint32_t i = 0; i < L.C; ++i) {
-        powc[i] = pow(10.0, th[L.c + i]);
-        csum += powc[i];
-    }
-    double acc = 0.0;
-    for (uint32_t i = 0; i < PCS_MAX_C; ++i) {
-        pd.pre_comp_prob[i] = 2.0f;
-        pd.sd_scale[i] = 0.0f;
-        pd.sd_shape[i] = 0.0f;
-        pd.half_az[i] = 0.0f;
-    }
-    for (uint32_t i = 0; i < L.C; ++i) {
-        acc += powc[i] / csum;
-        pd.pre_comp_prob[i] = (float)acc;
-        if (pm.model == PCS_DEV_MODEL_LOGNORMAL) {
-            /* lognormal diameter (nm) with mean mu, sd s: sigma_ln^2 = ln(1 + s^2/mu^2) */
-            const double mu = th[L.m + i], sdv = th[L.s + i];
-            const double sl2 = log1p((sdv * sdv) / (mu * mu));
-            const double mul = log(mu) - 0.5 * sl2;
-            pd.sd_scale[i] = (float)(pm.sd_const * exp(-0.5 * mul));
-            pd.sd_shape[i] = (float)(-0.5 * sqrt(sl2));
-        } else {
-            pd.sd_scale[i] = (float)sqrt(2.0 * th[L.m + i] * pm.delta_t);
-        }
-    }
-    pd.pre_comp_prob[L.C - 1] = 2.0f; /* simulation_impl.inl:331-335 */
-    for (uint32_t z = 0; z < L.Z; ++z) {
-        const float azf = (float)th[L.az + z];
-        pd.half_az[z] = (gen == 0u && pm.quirk_full_az) ? azf : 0.5f * azf;
-    }
-    const double lambda = csum * pm.volume_factor;
+    const double lambda = pcs_build_args(pm, th, gen, pd);
 
-    /* particle counts and their prefix */
     const uint64_t coff = (uint64_t)q * (2u * rd->v_max + 1u);
     uint32_t* cnt = a.counts + coff;
-    uint32_t* pre = cnt + jd.V;
-    uint64_t total = 0, steps = 0;
-    pre[0] = 0u;
-    for (uint32_t v = 0; v < jd.V; ++v) {
-        const uint32_t c = poisson_(lambda, v, slot, gt, k0, k1);
-        cnt[v] = c;
-        total += c;
-        steps += (uint64_t)c * jd.frames[v];
-        pre[v + 1] = (uint32_t)min(total, (uint64_t)0xFFFFFFFFu);
-    }
+    uint64_t steps = 0;
+    const uint64_t total = pcs_draw_counts(lambda, jd.V, jd.frames, slot, trial, gen, k0, k1, cnt, cnt + jd.V, &steps);
     if (total > 0xFFFFFFFFull) atomicOr(a.err, PCS_ERRBIT_COUNTS);
     pd.total_particles = (uint32_t)min(total, (uint64_t)0xFFFFFFFFu);
     pd.counts_off = coff;

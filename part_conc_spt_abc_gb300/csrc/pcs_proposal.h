@@ -1,0 +1,247 @@
+/*
+ * pcs_proposal.h -- construction of one ABC-PMC proposal, shared by the
+ * batched device path (k_propose) and the plain per-proposal host path
+ * (plain.cpp), so both draw the same parameters from the same streams.
+ *
+ * Follows the reference's proposal loop (src/gpu/detail/simulation_impl.inl
+ * :256-347): weighted parent pick (wrand_idx_ :54-62), reflected Gaussian
+ * displacement of every parameter (displace_ :64-79), components sorted by
+ * m (:276-303), 10^log10c, Poisson particle counts per video (:307-317),
+ * half depths, cumulative component probabilities with the last forced to 2
+ * (:319-335), step sd = sqrt(2 m dt) (:337-340).
+ */
+#ifndef PCS_PROPOSAL_H
+#define PCS_PROPOSAL_H
+
+#include <math.h>
+#include <stdint.h>
+
+#include "pcs_common.h"
+#include "pcs_kernels.h"
+
+namespace pcs {
+
+/* parameter layout: [m | s (lognormal) | log10c | az] */
+struct Layout {
+    uint32_t m, s, c, az, C, Z;
+};
+
+PCS_HD Layout pcs_layout(const JobPmcDev& pm)
+{
+    Layout L;
+    L.C = pm.C;
+    L.Z = pm.Z;
+    L.m = 0;
+    L.s = pm.C;
+    L.c = (pm.model == PCS_DEV_MODEL_LOGNORMAL) ? 2 * pm.C : pm.C;
+    L.az = L.c + pm.C;
+    return L;
+}
+
+/* standard normal pair from 4 words (Box-Muller in double) */
+PCS_HD void pcs_normal2(pcs_u4 r, double& n0, double& n1)
+{
+    const double u1 = 1.0 - pcs_u01_53(r.x, r.y); /* (0, 1] */
+    const double u2 = pcs_u01_53(r.z, r.w);
+    const double rad = sqrt(-2.0 * log(u1));
+    double s, c;
+#if defined(__CUDA_ARCH__)
+    sincospi(2.0 * u2, &s, &c);
+#else
+    s = sin(2.0 * 3.14159265358979323846 * u2);
+    c = cos(2.0 * 3.14159265358979323846 * u2);
+#endif
+    n0 = rad * s;
+    n1 = rad * c;
+}
+
+/* displace_ reflection, with a bounded loop and a closed-form fold after it */
+PCS_HD double pcs_reflect(double bis, double lo, double hi)
+{
+    for (int it = 0; it < 64 && (bis < lo || bis > hi); ++it) {
+        if (bis < lo) bis += 2.0 * (lo - bis);
+        if (bis > hi) bis -= 2.0 * (bis - hi);
+    }
+    if (bis < lo || bis > hi) {
+        const double w = hi - lo;
+        const double t = fmod(fabs(bis - lo), 2.0 * w);
+        bis = lo + (t <= w ? t : 2.0 * w - t);
+    }
+    return bis;
+}
+
+/* Poisson(lambda): inversion below 12, PTRS transformed rejection above
+ * (W. Hoermann, "The transformed rejection method for generating Poisson
+ * random variables", Insurance: Mathematics and Economics 12, 1993). */
+PCS_HD uint32_t pcs_poisson(double lam, uint32_t video, uint32_t slot, uint32_t gt, uint32_t k0, uint32_t k1)
+{
+    if (!(lam > 0.0)) return 0u;
+    if (lam < 12.0) {
+        const pcs_u4 r = pcs_philox(video, pcs_ctr_tag(PCS_STREAM_POISSON, 0u), slot, gt, k0, k1);
+        const double u = pcs_u01_53(r.x, r.y);
+        double p = exp(-lam), F = p;
+        uint32_t k = 0;
+        while (u > F && k < 1000u) {
+            ++k;
+            p *= lam / k;
+            F += p;
+        }
+        return k;
+    }
+    const double slam = sqrt(lam), loglam = log(lam);
+    const double b = 0.931 + 2.53 * slam;
+    const double a = -0.059 + 0.02483 * b;
+    const double invalpha = 1.1239 + 1.1328 / (b - 3.4);
+    const double vr = 0.9277 - 3.6224 / (b - 2.0);
+    for (uint32_t it = 0; it < 256u; ++it) {
+        const pcs_u4 r = pcs_philox(video, pcs_ctr_tag(PCS_STREAM_POISSON, 1u + it), slot, gt, k0, k1);
+        const double U = pcs_u01_53(r.x, r.y) - 0.5;
+        const double V = pcs_u01_53(r.z, r.w);
+        const double us = 0.5 - fabs(U);
+        const double kf = floor((2.0 * a / us + b) * U + lam + 0.43);
+        if (us >= 0.07 && V <= vr) return (uint32_t)kf;
+        if (kf < 0.0 || (us < 0.013 && V > us)) continue;
+        if (log(V) + log(invalpha) - log(a / (us * us) + b) <= -lam + kf * loglam - lgamma(kf + 1.0))
+            return (uint32_t)kf;
+    }
+    return (uint32_t)floor(lam + 0.5);
+}
+
+/* first cumulative weight >= u (std::lower_bound), clamped to N - 1 */
+PCS_HD uint32_t pcs_pick(const double* wcum, uint32_t N, double u)
+{
+    uint32_t lo = 0, hi = N;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (wcum[mid] < u)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo < N ? lo : N - 1;
+}
+
+/* Parameters of trial `trial` of population slot `slot` in generation `gen`.
+ * Generation 0 (the prior pass) simulates the slot's own parameters. */
+PCS_HD void pcs_build_theta(const JobPmcDev& pm, const double* theta_pop, const double* wcum,
+                            const double* factor, uint32_t slot, uint32_t trial, uint32_t gen,
+                            uint32_t k0, uint32_t k1, double* th)
+{
+    const uint32_t P = pm.P, N = pm.N;
+    const Layout L = pcs_layout(pm);
+    const uint32_t gt = pcs_ctr_gen_trial(gen, trial);
+    if (gen == 0u) {
+        for (uint32_t p = 0; p < P; ++p) th[p] = theta_pop[(uint64_t)slot * P + p];
+        return;
+    }
+    const pcs_u4 r = pcs_philox(0u, pcs_ctr_tag(PCS_STREAM_PICK, 0u), slot, gt, k0, k1);
+    const uint32_t parent = pcs_pick(wcum, N, pcs_u01_53(r.x, r.y));
+    const double* tp = theta_pop + (uint64_t)parent * P;
+    double nrm[PCS_MAX_P];
+    for (uint32_t p = 0; p < P; p += 2) {
+        const pcs_u4 rr = pcs_philox(p >> 1, pcs_ctr_tag(PCS_STREAM_PERTURB, 0u), slot, gt, k0, k1);
+        double n0, n1;
+        pcs_normal2(rr, n0, n1);
+        nrm[p] = n0;
+        if (p + 1 < P) nrm[p + 1] = n1;
+    }
+    for (uint32_t p = 0; p < P; ++p) {
+        if (pm.fixed[p]) {
+            th[p] = pm.lo[p];
+            continue;
+        }
+        double delta;
+        if (pm.perturbation == 1u) {
+            delta = 0.0;
+            for (uint32_t i = 0; i <= p; ++i)
+                if (!pm.fixed[i]) delta += factor[p * P + i] * nrm[i];
+        } else {
+            delta = factor[p * P + p] * nrm[p];
+        }
+        th[p] = pcs_reflect(tp[p] + delta, pm.lo[p], pm.hi[p]);
+    }
+    /* sort components by the first parameter group (label switching) */
+    for (uint32_t i = 1; i < L.C; ++i) {
+        for (uint32_t x = i; x > 0 && th[L.m + x] < th[L.m + x - 1]; --x) {
+            double t;
+            t = th[L.m + x];
+            th[L.m + x] = th[L.m + x - 1];
+            th[L.m + x - 1] = t;
+            t = th[L.c + x];
+            th[L.c + x] = th[L.c + x - 1];
+            th[L.c + x - 1] = t;
+            if (pm.model == PCS_DEV_MODEL_LOGNORMAL) {
+                t = th[L.s + x];
+                th[L.s + x] = th[L.s + x - 1];
+                th[L.s + x - 1] = t;
+            }
+            if (L.Z > 1u) {
+                t = th[L.az + x];
+                th[L.az + x] = th[L.az + x - 1];
+                th[L.az + x - 1] = t;
+            }
+        }
+    }
+}
+
+/* Forward-model arguments of a proposal; returns the Poisson mean per video. */
+PCS_HD double pcs_build_args(const JobPmcDev& pm, const double* th, uint32_t gen, PropDev& pd)
+{
+    const Layout L = pcs_layout(pm);
+    double powc[PCS_MAX_C], csum = 0.0;
+    for (uint32_t i = 0; i < L.C; ++i) {
+        powc[i] = pow(10.0, th[L.c + i]);
+        csum += powc[i];
+    }
+    for (uint32_t i = 0; i < PCS_MAX_C; ++i) {
+        pd.pre_comp_prob[i] = 2.0f;
+        pd.sd_scale[i] = 0.0f;
+        pd.sd_shape[i] = 0.0f;
+        pd.half_az[i] = 0.0f;
+    }
+    double acc = 0.0;
+    for (uint32_t i = 0; i < L.C; ++i) {
+        acc += powc[i] / csum;
+        pd.pre_comp_prob[i] = (float)acc;
+        if (pm.model == PCS_DEV_MODEL_LOGNORMAL) {
+            /* lognormal diameter (nm), mean mu and sd s: sigma_ln^2 = ln(1 + s^2 / mu^2) */
+            const double mu = th[L.m + i], sdv = th[L.s + i];
+            const double sl2 = log1p((sdv * sdv) / (mu * mu));
+            const double mul = log(mu) - 0.5 * sl2;
+            pd.sd_scale[i] = (float)(pm.sd_const * exp(-0.5 * mul));
+            pd.sd_shape[i] = (float)(-0.5 * sqrt(sl2));
+        } else {
+            pd.sd_scale[i] = (float)sqrt(2.0 * th[L.m + i] * pm.delta_t);
+        }
+    }
+    pd.pre_comp_prob[L.C - 1] = 2.0f;
+    for (uint32_t z = 0; z < L.Z; ++z) {
+        const float azf = (float)th[L.az + z];
+        pd.half_az[z] = (gen == 0u && pm.quirk_full_az) ? azf : 0.5f * azf;
+    }
+    return csum * pm.volume_factor;
+}
+
+/* Poisson counts per video and their prefix; returns total particles (and
+ * particle-steps through *steps). */
+PCS_HD uint64_t pcs_draw_counts(double lambda, uint32_t V, const uint32_t* frames, uint32_t slot,
+                                uint32_t trial, uint32_t gen, uint32_t k0, uint32_t k1, uint32_t* cnt,
+                                uint32_t* pre, uint64_t* steps)
+{
+    const uint32_t gt = pcs_ctr_gen_trial(gen, trial);
+    uint64_t total = 0, st = 0;
+    pre[0] = 0u;
+    for (uint32_t v = 0; v < V; ++v) {
+        const uint32_t c = pcs_poisson(lambda, v, slot, gt, k0, k1);
+        cnt[v] = c;
+        total += c;
+        st += (uint64_t)c * frames[v];
+        pre[v + 1] = (uint32_t)(total < 0xFFFFFFFFull ? total : 0xFFFFFFFFull);
+    }
+    if (steps) *steps = st;
+    return total;
+}
+
+} // namespace pcs
+
+#endif
