@@ -301,3 +301,35 @@ def philox(ctr, key):
     out = np.zeros(4, np.uint32)
     lib().orc_philox4x32_10(ptr(c, C.c_uint32), ptr(k, C.c_uint32), ptr(out, C.c_uint32))
     return out
+
+
+class OrcAbcProblem(C.Structure):
+    _fields_ = [
+        ("C", C.c_uint32), ("N", C.c_uint32), ("generations", C.c_uint32), ("kmin", C.c_uint32),
+        ("V", C.c_uint32), ("R", C.c_uint32), ("B", C.c_uint32), ("quantile", C.c_double),
+        ("lb_m", C.c_double), ("ub_m", C.c_double), ("lb_s", C.c_double), ("ub_s", C.c_double),
+        ("lb_c", C.c_double), ("ub_c", C.c_double), ("az", C.c_double), ("Lx", C.c_double), ("Ly", C.c_double),
+        ("Lz", C.c_double), ("ax", C.c_double), ("ay", C.c_double), ("deltat", C.c_double), ("ub_de", C.c_double),
+        ("temperature", C.c_double), ("viscosity", C.c_double), ("frames", _u32p), ("ref_sat", _u32p),
+    ]
+
+
+def abc_pmc(problem: dict, frames, ref_sat, seed: int, nthreads: int):
+    """Whole ABC-PMC estimation on the CPU (abc_oracle.c).  Returns
+    (theta [N, 3C+1] with layout m | s | log10c | az, w [N], trials)."""
+    L = lib()
+    L.orc_abc_pmc.argtypes = [C.POINTER(OrcAbcProblem), C.c_uint64, C.c_uint32, _f64p, _f64p]
+    L.orc_abc_pmc.restype = C.c_uint64
+    fr = np.ascontiguousarray(frames, np.uint32)
+    sat = np.ascontiguousarray(ref_sat, np.uint32)
+    pb = OrcAbcProblem()
+    for k, v in problem.items():
+        setattr(pb, k, v)
+    pb.V, pb.R, pb.B = len(fr), sat.shape[0], sat.shape[1]
+    pb.frames = ptr(fr, C.c_uint32)
+    pb.ref_sat = ptr(sat, C.c_uint32)
+    P = 3 * problem["C"] + 1
+    th = np.zeros((problem["N"], P))
+    w = np.zeros(problem["N"])
+    trials = L.orc_abc_pmc(C.byref(pb), seed, nthreads, ptr(th, C.c_double), ptr(w, C.c_double))
+    return th, w, int(trials)

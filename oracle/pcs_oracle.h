@@ -178,6 +178,19 @@ typedef struct orc_cpu_job {
 uint64_t orc_cpu_forward_batch(const orc_cpu_job* jobs, uint32_t n_jobs, uint32_t nthreads,
                                uint64_t seed, double* seconds, uint64_t* checksum);
 
+/* An independent CPU run of a whole ABC-PMC estimation (abc_oracle.c):
+ * lognormal model, quantile schedule, pmc-standard weights. */
+typedef struct orc_abc_problem {
+    uint32_t C, N, generations, kmin, V, R, B;
+    double quantile;
+    double lb_m, ub_m, lb_s, ub_s, lb_c, ub_c; /* c in particles/ml */
+    double az, Lx, Ly, Lz, ax, ay, deltat, ub_de, temperature, viscosity;
+    const uint32_t* frames;  /* [V] */
+    const uint32_t* ref_sat; /* [R*B] */
+} orc_abc_problem;
+uint64_t orc_abc_pmc(const orc_abc_problem* pb, uint64_t seed, uint32_t nthreads, double* theta_out,
+                     double* w_out);
+
 #ifdef __cplusplus
 }
 #endif
