@@ -214,8 +214,16 @@ int orc_simulate_philox(const orc_setup* s, const orc_run* r, uint64_t seed, uin
 {
     orc_track_counts local = {0, 0};
     if (!counts) counts = &local;
-    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    const uint32_t gt = (generation << 20) | (trial & 0xFFFFFu);
+    /* fixed key, seed folded into counter words 2 and 3 through the
+     * splitmix64 finaliser (the product's stream layout) */
+    const uint32_t key[2] = {0xA4093822u, 0x299F31D0u};
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const uint32_t m0 = (uint32_t)z, m1 = (uint32_t)(z >> 32);
+    const uint32_t gt = ((generation << 20) | (trial & 0xFFFFFu)) ^ m1;
+    slot ^= m0;
     uint32_t n = 0;
     for (uint32_t v = 0; v < s->video_count; ++v) {
         const uint32_t frames = r->frames[v];

@@ -514,8 +514,7 @@ pcs_status pcs_simulate_hist(pcs_ctx* ctx, const pcs_setup* setup, const pcs_run
         jd.model = (uint32_t)setup->model;
         jd.C = Cc;
         jd.Z = setup->model == PCS_MODEL_DISCRETE_VARIABLE_DEPTH ? Cc : 1u;
-        jd.seed_lo = (uint32_t)seed;
-        jd.seed_hi = (uint32_t)(seed >> 32);
+        pcs_seed_masks(seed, &jd.seed_lo, &jd.seed_hi);
         jd.frames_max = fmax;
         uint32_t* d_frames = t.get<uint32_t>(V);
         PCS_CUDA(cudaMemcpyAsync(d_frames, setup->frames, V * 4u, cudaMemcpyHostToDevice, st));

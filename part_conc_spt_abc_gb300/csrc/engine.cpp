@@ -211,8 +211,7 @@ void Job::build_device_state()
     jd.C = C;
     jd.Z = Z;
     jd.P = P;
-    jd.seed_lo = (uint32_t)seed;
-    jd.seed_hi = (uint32_t)(seed >> 32);
+    pcs_seed_masks(seed, &jd.seed_lo, &jd.seed_hi);
     jd.frames_max = R - 1;
     jd.frames = d_frames;
     jd.ref_sat = d_sat;
@@ -266,7 +265,7 @@ void Job::build_device_state()
     std::vector<double> theta(nP), w(N, 1.0 / N), wcum(N), factor((size_t)P * P, 0.0);
     for (uint32_t s = 0; s < N; ++s)
         for (uint32_t q = 0; q < P; q += 2) {
-            pcs_u4 r = pcs_philox(q >> 1, pcs_ctr_tag(PCS_STREAM_PRIOR, 0u), s, pcs_ctr_gen_trial(0, 0),
+            pcs_u4 r = pcs_draw(q >> 1, pcs_ctr_tag(PCS_STREAM_PRIOR, 0u), s, pcs_ctr_gen_trial(0, 0),
                                   jd.seed_lo, jd.seed_hi);
             double u0 = pcs_u01_53(r.x, r.y), u1 = pcs_u01_53(r.z, r.w);
             theta[(uint64_t)s * P + q] = pm.lo[q] + (pm.hi[q] - pm.lo[q]) * u0;

@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
                         u2 = u[2];
                         u3 = u[3];
                     } else {
-                        pcs_u4 r = pcs_philox(n, pcs_ctr_tag(PCS_STREAM_PARTICLE, 0u), slot, gt, k0, k1);
+                        pcs_u4 r = pcs_draw(n, pcs_ctr_tag(PCS_STREAM_PARTICLE, 0u), slot, gt, k0, k1);
                         u0 = pcs_u01_24(r.x);
                         u1 = pcs_u01_24(r.y);
                         u2 = pcs_u01_24(r.z);
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
                         if (REPLAY) {
                             q.sd = a.rp_sigmas[n];
                         } else {
-                            pcs_u4 r = pcs_philox(n, pcs_ctr_tag(PCS_STREAM_PARTICLE, 1u), slot, gt, k0, k1);
+                            pcs_u4 r = pcs_draw(n, pcs_ctr_tag(PCS_STREAM_PARTICLE, 1u), slot, gt, k0, k1);
                             float z0, z1;
                             box_muller_(r.x, r.y, z0, z1);
                             q.sd = s_prop.sd_scale[comp] * expf(s_prop.sd_shape[comp] * z0);
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
                     } else {
 #pragma unroll
                         for (int b = 0; b < 3; ++b) {
-                            pcs_u4 r = pcs_philox(q.n, pcs_ctr_tag(PCS_STREAM_PARTICLE, 2u + 3u * g + (uint32_t)b), slot, gt, k0, k1);
+                            pcs_u4 r = pcs_draw(q.n, pcs_ctr_tag(PCS_STREAM_PARTICLE, 2u + 3u * g + (uint32_t)b), slot, gt, k0, k1);
                             box_muller_(r.x, r.y, nn[4 * b + 0], nn[4 * b + 1]);
                             box_muller_(r.z, r.w, nn[4 * b + 2], nn[4 * b + 3]);
                         }
@@ -374,7 +374,7 @@ int simulate_occupancy(const SimLaunch& l, uint32_t tile_words)
 __global__ void k_debug_stream(uint32_t k0, uint32_t k1, uint32_t slot, uint32_t gt, uint32_t n,
                                uint32_t j, uint32_t* out)
 {
-    pcs_u4 r = pcs_philox(n, pcs_ctr_tag(PCS_STREAM_PARTICLE, j), slot, gt, k0, k1);
+    pcs_u4 r = pcs_draw(n, pcs_ctr_tag(PCS_STREAM_PARTICLE, j), slot, gt, k0, k1);
     out[0] = r.x;
     out[1] = r.y;
     out[2] = r.z;
@@ -384,8 +384,9 @@ __global__ void k_debug_stream(uint32_t k0, uint32_t k1, uint32_t slot, uint32_t
 cudaError_t launch_debug_stream(uint64_t seed, uint32_t slot, uint32_t gen, uint32_t trial,
                                 uint32_t particle, uint32_t block, uint32_t* d_out, cudaStream_t st)
 {
-    k_debug_stream<<<1, 1, 0, st>>>((uint32_t)seed, (uint32_t)(seed >> 32), slot,
-                                    pcs_ctr_gen_trial(gen, trial), particle, block, d_out);
+    uint32_t m0 = 0, m1 = 0;
+    pcs_seed_masks(seed, &m0, &m1);
+    k_debug_stream<<<1, 1, 0, st>>>(m0, m1, slot, pcs_ctr_gen_trial(gen, trial), particle, block, d_out);
     return cudaGetLastError();
 }
 

@@ -92,6 +92,30 @@ PCS_HD pcs_u4 pcs_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uin
     return o;
 }
 
+/* Every stream of the engine uses one fixed Philox key (so the ten round
+ * keys are compile-time constants) and folds the job seed into counter words
+ * 2 and 3 through two 32-bit masks from the splitmix64 finaliser of the seed.
+ * Within a job the map (slot, generation|trial) -> counter is a bijection, so
+ * no two draws of a job share a counter; jobs with different seeds get
+ * unrelated masks. */
+#define PCS_PHILOX_K0 0xA4093822u
+#define PCS_PHILOX_K1 0x299F31D0u
+
+PCS_HD void pcs_seed_masks(uint64_t seed, uint32_t* m0, uint32_t* m1)
+{
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    *m0 = (uint32_t)z;
+    *m1 = (uint32_t)(z >> 32);
+}
+
+PCS_HD pcs_u4 pcs_draw(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t m0, uint32_t m1)
+{
+    return pcs_philox(c0, c1, c2 ^ m0, c3 ^ m1, PCS_PHILOX_K0, PCS_PHILOX_K1);
+}
+
 /* counter word 3: generation (12 bits) and trial (20 bits) */
 PCS_HD uint32_t pcs_ctr_gen_trial(uint32_t gen, uint32_t trial)
 {

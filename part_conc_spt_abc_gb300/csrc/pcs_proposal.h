@@ -77,7 +77,7 @@ PCS_HD uint32_t pcs_poisson(double lam, uint32_t video, uint32_t slot, uint32_t 
 {
     if (!(lam > 0.0)) return 0u;
     if (lam < 12.0) {
-        const pcs_u4 r = pcs_philox(video, pcs_ctr_tag(PCS_STREAM_POISSON, 0u), slot, gt, k0, k1);
+        const pcs_u4 r = pcs_draw(video, pcs_ctr_tag(PCS_STREAM_POISSON, 0u), slot, gt, k0, k1);
         const double u = pcs_u01_53(r.x, r.y);
         double p = exp(-lam), F = p;
         uint32_t k = 0;
@@ -94,7 +94,7 @@ PCS_HD uint32_t pcs_poisson(double lam, uint32_t video, uint32_t slot, uint32_t 
     const double invalpha = 1.1239 + 1.1328 / (b - 3.4);
     const double vr = 0.9277 - 3.6224 / (b - 2.0);
     for (uint32_t it = 0; it < 256u; ++it) {
-        const pcs_u4 r = pcs_philox(video, pcs_ctr_tag(PCS_STREAM_POISSON, 1u + it), slot, gt, k0, k1);
+        const pcs_u4 r = pcs_draw(video, pcs_ctr_tag(PCS_STREAM_POISSON, 1u + it), slot, gt, k0, k1);
         const double U = pcs_u01_53(r.x, r.y) - 0.5;
         const double V = pcs_u01_53(r.z, r.w);
         const double us = 0.5 - fabs(U);
@@ -134,12 +134,12 @@ PCS_HD void pcs_build_theta(const JobPmcDev& pm, const double* theta_pop, const 
         for (uint32_t p = 0; p < P; ++p) th[p] = theta_pop[(uint64_t)slot * P + p];
         return;
     }
-    const pcs_u4 r = pcs_philox(0u, pcs_ctr_tag(PCS_STREAM_PICK, 0u), slot, gt, k0, k1);
+    const pcs_u4 r = pcs_draw(0u, pcs_ctr_tag(PCS_STREAM_PICK, 0u), slot, gt, k0, k1);
     const uint32_t parent = pcs_pick(wcum, N, pcs_u01_53(r.x, r.y));
     const double* tp = theta_pop + (uint64_t)parent * P;
     double nrm[PCS_MAX_P];
     for (uint32_t p = 0; p < P; p += 2) {
-        const pcs_u4 rr = pcs_philox(p >> 1, pcs_ctr_tag(PCS_STREAM_PERTURB, 0u), slot, gt, k0, k1);
+        const pcs_u4 rr = pcs_draw(p >> 1, pcs_ctr_tag(PCS_STREAM_PERTURB, 0u), slot, gt, k0, k1);
         double n0, n1;
         pcs_normal2(rr, n0, n1);
         nrm[p] = n0;

@@ -84,8 +84,14 @@ def test_philox_stream_layout(pcs, ctx, oracle):
     for seed, slot, trial, gen, n, blk in [(0, 0, 0, 0, 0, 0), (0xDEADBEEF12345678, 17, 3, 5, 999, 2),
                                            (42, 4095, 0xFFFFF, 4095, 123456, 77)]:
         got = pcs.debug_particle_stream(ctx, seed, slot, trial, gen, n, blk)
-        ctr = [n, (0 << 28) | blk, slot, (gen << 20) | trial]
-        want = oracle.philox(ctr, [seed & 0xFFFFFFFF, seed >> 32])
+        # fixed key; the seed enters counter words 2 and 3 through splitmix64 masks
+        M = (1 << 64) - 1
+        z = (seed + 0x9E3779B97F4A7C15) & M
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+        z ^= z >> 31
+        ctr = [n, (0 << 28) | blk, slot ^ (z & 0xFFFFFFFF), ((gen << 20) | trial) ^ (z >> 32)]
+        want = oracle.philox(ctr, [0xA4093822, 0x299F31D0])
         assert np.array_equal(got, want)
 
 
