@@ -177,7 +177,8 @@ pcs_status pcs_job_create(pcs_ctx* ctx, const pcs_params* p, const pcs_observed*
                           uint64_t seed, pcs_job** out);
 pcs_status pcs_job_destroy(pcs_job* job);
 /* Runs to convergence, or for max_steps generations when max_steps > 0
- * (accel -S).  Blocking; one job at a time (the plain form). */
+ * (accel -S).  max_steps = 0 keeps the job's pcs_params.max_generations
+ * (0 there too: no cap).  Blocking. */
 pcs_status pcs_job_run(pcs_job* job, uint32_t max_steps);
 /* The plain form: the reference's schedule (host-side PMC in double, one
  * proposal per simulate + distance launch, `queues` streams in flight, at most

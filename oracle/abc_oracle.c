@@ -15,6 +15,7 @@
  * the previous generation's distances (prior pass for the first).
  */
 #include <math.h>
+#include <stdio.h>
 #include <pthread.h>
 #include <stdatomic.h>
 #include <stdint.h>
@@ -316,6 +317,13 @@ uint64_t orc_abc_pmc(const orc_abc_problem* pb, uint64_t seed, uint32_t nthreads
             memcpy(c.dist, c.dist_new, sizeof(double) * N);
         }
         c.gamma = quantile_of(c.dist, N, pb->quantile);
+        if (getenv("PCS_ORACLE_TRACE")) {
+            double ess = 0.0, s2 = 0.0;
+            for (uint32_t i = 0; i < N; ++i) s2 += c.w[i] * c.w[i];
+            ess = 1.0 / s2;
+            fprintf(stderr, "oracle abc: generation %u gamma %.4f trials %llu ess %.1f\n", gen, c.gamma,
+                    (unsigned long long)atomic_load(&c.trials), ess);
+        }
     }
     memcpy(theta_out, c.theta, sizeof(double) * N * P);
     memcpy(w_out, c.w, sizeof(double) * N);

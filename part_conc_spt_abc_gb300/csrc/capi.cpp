@@ -341,7 +341,7 @@ pcs_status pcs_job_run(pcs_job* job, uint32_t max_steps)
         Job& j = J_(job);
         PCS_CUDA(cudaSetDevice(j.ctx->device));
         if (!j.initialised) {
-            j.p.max_generations = max_steps;
+            if (max_steps) j.p.max_generations = max_steps;
         } else if (max_steps) {
             throw Error(PCS_ERR_INVALID_ARGUMENT, "max_steps must be set before the job's first step");
         }

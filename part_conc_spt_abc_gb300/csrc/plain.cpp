@@ -51,7 +51,7 @@ void run_plain(Job& j, uint32_t max_steps, uint32_t queues)
     Ctx& c = *j.ctx;
     if (j.slot >= 0) throw Error(PCS_ERR_BUSY, "job is admitted to the batched engine");
     if (!j.initialised) {
-        j.p.max_generations = max_steps;
+        if (max_steps) j.p.max_generations = max_steps;
         j.build_device_state();
     } else if (j.status.iterations > 0) {
         throw Error(PCS_ERR_INVALID_ARGUMENT, "the plain form runs a job from its start");

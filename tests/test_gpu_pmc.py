@@ -121,6 +121,14 @@ def test_max_steps_semantics(pcs, ctx):
     info = sim.info()
     assert info.iterations == 3 and not info.converged
     sim.close()
+    # run(0) keeps the cap the job's parameters carry
+    inp.params.max_generations = 2
+    for plain in (False, True):
+        sim = pcs.make_simulation(ctx, inp, 1)
+        sim.run_plain() if plain else sim.run()
+        info = sim.info()
+        assert info.iterations == 3 and not info.converged, plain
+        sim.close()
 
 
 def test_accel_end_to_end(pcs, ctx, tmp_path):
