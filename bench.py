@@ -39,6 +39,17 @@ OPS_PER_STEP = 113
 DIST_BYTES_PER_CELL = 12
 WORKLOAD = ("config1: 2-component lognormal (175/500 nm, sd 10/25, w 0.6/0.4), 5e14 m^-3, "
             "50 videos x 300 frames, pop 1024, quantile-0.5 schedule, R x B = 301 x 128")
+WORKLOADS = {
+    0: ("config0: 1-component lognormal (175 nm, sd 10), 2e14 m^-3, 20 videos x 200 frames, pop 256, "
+        "quantile-0.5 schedule, R x B = 201 x 100", "one ABC-PMC generation"),
+    1: (WORKLOAD, "one ABC-PMC generation"),
+    2: ("config2: 2-component lognormal, diameters U(100,800) nm, concentration prior spanning 50..5000 "
+        "particles per video, 20 videos x 200 frames, pop 512, 512 proposals per round, R x B = 201 x 100",
+        "one ABC-PMC generation (512-proposal rounds)"),
+    3: ("config3: 3-component lognormal (100/250/600 nm, sd 5%, w 0.3/0.4/0.3), 1e5 particles per video, "
+        "100 videos x 1000 frames, pop 4096, R x B = 1001 x 256",
+        "one round of 64 prior-pass proposals (fixed slice; a full run is ~4e14 particle-steps)"),
+}
 
 
 def measured_peaks():
@@ -170,18 +181,10 @@ def run_reference(args, rank, world):
     barrier(world)
 
 
-def run_serve(args, rank, world):
-    """The serving stream (BASELINE configuration 4): jobs arrive as a
-    Poisson process at 2 jobs/s; the served form admits them into the
-    continuous-batching loop as they arrive, the plain form runs them one at
-    a time in arrival order with the reference's per-proposal schedule."""
-    import part_conc_spt_abc_gb300 as P
-    import part_conc_spt_abc_gb300.workloads as W
-    ctx = P.Context(rank)
-    jobs, arrivals = W.serve_stream(ctx, n_jobs=args.jobs, seed=args.seed)
+def serve_stream_run(P, ctx, jobs, arrivals):
+    """Served form: jobs are submitted at their arrival offsets into the
+    continuous-batching loop.  Returns latency percentiles and totals."""
     n = len(jobs)
-    res = {}
-    # ---- served -----------------------------------------------------------
     srv = P.Server(ctx)
     sims = [P.make_simulation(ctx, j[0], j[2]) for j in jobs]
     finish = [None] * n
@@ -202,49 +205,88 @@ def run_serve(args, rank, world):
         if active == 0 and submitted < n:
             time.sleep(max(0.0, min(0.05, arrivals[submitted] - now)))
     makespan = max(finish)
-    lat = np.array(finish) - arrivals
+    lat = np.array(finish) - np.asarray(arrivals[:n])
     acc = sum(s.info().accepted for s in sims)
     props = sum(s.info().simulations for s in sims)
     steps = sum(s.info().particle_steps for s in sims)
-    res["served"] = {"jobs": n, "makespan_s": makespan, "p50_latency_s": float(np.percentile(lat, 50)),
-                     "p99_latency_s": float(np.percentile(lat, 99)), "accepted_per_s": acc / makespan,
-                     "proposals_per_s": props / makespan, "particle_steps_per_s": steps / makespan}
     for s in sims:
         s.close()
-    # ---- plain: one job at a time, reference schedule ----------------------
-    clock = 0.0
-    lat_p, acc_p, props_p, steps_p, done = [], 0, 0, 0, 0
+    return {"jobs": n, "makespan_s": makespan, "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "accepted": int(acc), "accepted_per_s": acc / makespan,
+            "proposals_per_s": props / makespan, "particle_steps_per_s": steps / makespan}
+
+
+def plain_stream_run(P, ctx, jobs, arrivals, budget_s, geometry):
+    """Plain form: jobs one at a time in arrival order, each with the
+    reference's per-proposal schedule (30 queues), until the budget is spent.
+    The clock is simulated: a job starts at max(its arrival, the previous
+    job's end)."""
+    ctx.set_tuning(plain_launch=geometry)
+    clock, lat, acc, props, steps, done = 0.0, [], 0, 0, 0, 0
     t_start = time.perf_counter()
     for i, (inp, truth, seed) in enumerate(jobs):
-        if time.perf_counter() - t_start > args.plain_budget:
+        if time.perf_counter() - t_start > budget_s:
             break
         sim = P.make_simulation(ctx, inp, seed)
         t = time.perf_counter()
         sim.run_plain(0, 30)
         dt = time.perf_counter() - t
         clock = max(clock, arrivals[i]) + dt
-        lat_p.append(clock - arrivals[i])
+        lat.append(clock - arrivals[i])
         inf = sim.info()
-        acc_p += inf.accepted
-        props_p += inf.simulations
-        steps_p += inf.particle_steps
+        acc += inf.accepted
+        props += inf.simulations
+        steps += inf.particle_steps
         done += 1
         sim.close()
-    busy = time.perf_counter() - t_start
-    res["plain"] = {"jobs_completed": done, "makespan_s": clock, "busy_s": busy,
-                    "p50_latency_s": float(np.percentile(lat_p, 50)) if lat_p else None,
-                    "p99_latency_s": float(np.percentile(lat_p, 99)) if lat_p else None,
-                    "accepted_per_s": acc_p / max(clock, 1e-9), "proposals_per_s": props_p / max(clock, 1e-9),
-                    "particle_steps_per_s": steps_p / max(clock, 1e-9),
-                    "note": "accepted/s over the completed jobs' simulated-arrival makespan"}
-    # same-jobs comparison when plain did not finish them all
-    sub = done
-    res["served_over_plain_accepted_per_s"] = res["served"]["accepted_per_s"] / max(res["plain"]["accepted_per_s"], 1e-12)
+    ctx.set_tuning(plain_launch=1)
+    return {"jobs": done, "makespan_s": clock, "p50_latency_s": float(np.percentile(lat, 50)) if lat else None,
+            "p99_latency_s": float(np.percentile(lat, 99)) if lat else None, "accepted": int(acc),
+            "accepted_per_s": acc / max(clock, 1e-9), "proposals_per_s": props / max(clock, 1e-9),
+            "particle_steps_per_s": steps / max(clock, 1e-9)}
+
+
+def run_serve(args, rank, world):
+    """The serving stream (BASELINE configuration 4): jobs arrive as a
+    Poisson process at 2 jobs/s.  The served form admits them into the
+    continuous-batching loop as they arrive (headline: p50/p99 latency and
+    accepted proposals/s over the whole stream).  The plain form runs jobs
+    one at a time in arrival order with the reference's per-proposal
+    schedule; it cannot finish the stream in minutes, so the served/plain
+    ratio is taken on equal work: the first --cmp-jobs jobs of the stream,
+    each capped at --cmp-generations generations after the prior pass, same
+    arrival offsets, run by the plain form (reference launch geometry, and
+    this build's persistent grid) and by the served form."""
+    import part_conc_spt_abc_gb300 as P
+    import part_conc_spt_abc_gb300.workloads as W
+    ctx = P.Context(rank)
+    jobs, arrivals = W.serve_stream(ctx, n_jobs=args.jobs, seed=args.seed)
+    res = {"served": serve_stream_run(P, ctx, jobs, arrivals)}
+    cmp_jobs = []
+    for inp, truth, seed in jobs[:args.cmp_jobs]:
+        inp.params.max_generations = args.cmp_generations
+        cmp_jobs.append((inp, truth, seed))
+    cmp_arr = arrivals[:len(cmp_jobs)]
+    comparisons = {}
+    for name, geometry in (("reference_launch", 1), ("persistent_grid", 2)):
+        plain = plain_stream_run(P, ctx, cmp_jobs, cmp_arr, args.plain_budget, geometry)
+        J = plain["jobs"]
+        if J == 0:
+            comparisons[name] = {"plain": plain}
+            continue
+        served_j = serve_stream_run(P, ctx, cmp_jobs[:J], cmp_arr[:J])
+        comparisons[name] = {"plain": plain, "served_same_jobs": served_j,
+                             "served_over_plain_accepted_per_s":
+                                 served_j["accepted_per_s"] / max(plain["accepted_per_s"], 1e-12)}
+    res["equal_work"] = comparisons
     line = {"metric": "serve p50/p99 job latency, accepted proposals/s (served vs plain)",
             "value": res["served"]["accepted_per_s"], "unit": "accepted proposals/s", "n_gpus": 1,
-            "config": {"workload": f"serving stream: {n} jobs, Poisson arrivals 2/s, 1-3 lognormal components, "
-                                   "100-500 frames, 64-256 DE bins, pop 256-4096, 6-12 generations",
-                       "plain_jobs_compared": sub},
+            "config": {"workload": f"serving stream: {len(jobs)} jobs, Poisson arrivals 2/s, 1-3 lognormal "
+                                   "components, 100-500 frames, 64-256 DE bins, pop 256-4096, 6-12 generations",
+                       "equal_work": f"first {len(cmp_jobs)} jobs, {args.cmp_generations} generations after the "
+                                     f"prior pass each, plain budget {args.plain_budget:.0f} s per form",
+                       "plain_forms": "reference_launch: ceil(V/4) CTAs x 128 threads per proposal, as the "
+                                      "reference launches its kernel; persistent_grid: this build's grid"},
             **res}
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -259,10 +301,14 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="configuration 0 (pop 256): the case profiled under ncu")
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3],
+                    help="benchmark configuration (1 is the headline; 3 times a fixed 64-proposal slice)")
     ap.add_argument("--serve", action="store_true", help="the 64-job serving stream, served vs plain")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--plain-budget", type=float, default=600.0, help="seconds allowed for the plain form")
+    ap.add_argument("--plain-budget", type=float, default=300.0, help="seconds allowed for each plain form")
+    ap.add_argument("--cmp-jobs", type=int, default=8, help="serve: jobs in the equal-work comparison")
+    ap.add_argument("--cmp-generations", type=int, default=2, help="serve: generations per compared job")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -279,25 +325,41 @@ def main():
 
     peaks, peak_src = measured_peaks()
     ctx = P.Context(local)
+    cfg = 0 if args.small else args.config
+    workload, step_def = WORKLOADS[cfg]
     gens = args.warmup + args.steps + 2
-    inp, truth = (W.config0 if args.small else W.config1)(ctx, seed=0, generations=gens)
-    tune = None
-    if not args.no_autotune:
-        t = ctx.autotune(inp)
-        tune = dict(block=t.block_size, ppt=t.particles_per_thread, tile_rows=t.hist_tile_rows,
-                    warp_aggregate=t.warp_aggregate, chunk=t.chunk_particles, capacity=t.round_capacity)
+    inp, truth = {0: W.config0, 1: W.config1, 2: W.config2, 3: W.config3}[cfg](ctx, seed=0, generations=gens)
+    if not args.no_autotune and cfg != 3:
+        ctx.autotune(inp)
+    if cfg == 2:
+        ctx.set_tuning(round_capacity=512)
+    if cfg == 3:
+        ctx.set_tuning(round_capacity=64)
+    t = ctx.tuning
+    tune = dict(block=t.block_size, ppt=t.particles_per_thread, tile_rows=t.hist_tile_rows,
+                warp_aggregate=t.warp_aggregate, chunk=t.chunk_particles, capacity=t.round_capacity,
+                autotuned=not args.no_autotune and cfg != 3)
+
+    def stepper(sim):
+        """advance one step: a generation, or one round of the fixed slice"""
+        if cfg != 3:
+            return sim.step
+        srv = P.Server(ctx)
+        srv.submit(sim)
+        return srv.step
 
     # ---- device-resident run: inputs already in HBM -----------------------
     sim = P.make_simulation(ctx, inp, seed=1 + rank)
+    step = stepper(sim)
     for _ in range(args.warmup):
-        sim.step()
+        step()
     barrier(world)
     ctx.reset_kernel_stats()
     i0 = sim.info()
     clocks = Clocks(local)
     ctx.timer_start()
     for _ in range(args.steps):
-        sim.step()
+        step()
     ms = ctx.timer_stop()
     clk = clocks.stop()
     i1 = sim.info()
@@ -316,9 +378,10 @@ def main():
     barrier(world)
     t0 = time.perf_counter()
     sim2 = P.make_simulation(ctx, inp, seed=101 + rank)  # H2D: observed K, DE, frame counts
+    step2 = stepper(sim2)
     d2h = 0
     for _ in range(args.steps):
-        sim2.step()
+        step2()
         out = sim2.output()  # D2H: the population (m, s, c, az, dist, w)
         d2h = sum(a.nbytes for a in (out.m, out.c, out.az, out.dist, out.w, out.s) if a is not None)
     e2e_s = time.perf_counter() - t0
@@ -344,12 +407,15 @@ def main():
     dist_ms = ks.distance_ms / max(1, ks.distance_launches)
     dist_gbs = (ks.histogram_cells / max(1, ks.distance_launches)) * DIST_BYTES_PER_CELL / (dist_ms / 1e3) / 1e9
 
+    cells = ks.histogram_cells / max(1, ks.rounds)
+    l2_note = (f"round histograms {cells * 4 / 1e6:.0f} MB per round + job state"
+               + (" (above L2)" if cells * 4 > 129e6 else " (below L2; the kernels are issue-bound)"))
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "step": "one ABC-PMC generation", "parallelism": f"replicas x{world}",
-                   "l2": "working set above L2 (round histograms ~315 MB + job state)", "tuning": tune},
+        "config": {"workload": workload, "step": step_def, "parallelism": f"replicas x{world}",
+                   "l2": l2_note, "tuning": tune},
         "proposals_per_s": props_all / (ms_max / 1e3),
         "accepted_per_s": acc_all / (ms_max / 1e3),
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
@@ -367,7 +433,9 @@ def main():
                       "rounds": int(ks.rounds), "round_ms_total": ks.round_ms},
         "clocks": clk,
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if cfg != 1:
+        line["config"]["headline"] = False
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and cfg == 1:
         threads = os.cpu_count() or 1
         sample, n = cpu_port_sample(10.0, threads)
         st, s = sample(7)

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define PCS_ABI_VERSION 1
+#define PCS_ABI_VERSION 2
 #define PCS_MAX_COMPONENTS 8
 
 typedef enum pcs_status {
@@ -131,16 +131,23 @@ int pcs_abi_version(void);
  * returns the length written (truncated to cap - 1). */
 size_t pcs_device_report(char* buf, size_t cap);
 
-/* Tuning knobs (0 keeps the current / autotuned value). */
+/* Tuning knobs.  In pcs_set_tuning a field of 0 keeps the current /
+ * autotuned value; PCS_TUNE_ZERO sets a field to 0 where 0 is meaningful
+ * (hist_tile_rows, warp_aggregate, use_graphs).  pcs_get_tuning reports
+ * plain values. */
+#define PCS_TUNE_ZERO 0xFFFFFFFFu
 typedef struct pcs_tuning {
     uint32_t block_size;          /* forward-model threads per CTA */
     uint32_t particles_per_thread;/* independent walkers interleaved per thread: 1, 2 or 4 */
     uint32_t hist_tile_rows;      /* histogram rows privatised in shared memory */
-    uint32_t warp_aggregate;      /* 1: warp-aggregated shared atomics, 0: plain, 2: auto */
+    uint32_t warp_aggregate;      /* 1: warp-aggregated shared atomics, 0: plain */
     uint32_t chunk_particles;     /* particles per work item */
     uint32_t round_capacity;      /* proposals per batched round */
     uint32_t max_speculation;     /* max trials per slot per round */
-    uint32_t use_graphs;          /* 1: capture rounds in CUDA graphs */
+    uint32_t use_graphs;          /* 1: capture rounds in CUDA graphs, 0: direct launches */
+    uint32_t plain_launch;        /* pcs_job_run_plain's simulate launch: 1 the reference's
+                                   * geometry (ceil(V/4) CTAs x 128 threads per proposal,
+                                   * default), 2 this build's persistent grid */
 } pcs_tuning;
 pcs_status pcs_get_tuning(pcs_ctx* ctx, pcs_tuning* out);
 pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t);

@@ -204,6 +204,7 @@ pcs_status pcs_get_tuning(pcs_ctx* ctx, pcs_tuning* out)
         out->round_capacity = c.tune.capacity;
         out->max_speculation = c.tune.max_spec;
         out->use_graphs = c.tune.use_graphs;
+        out->plain_launch = c.tune.plain_launch;
     });
 }
 
@@ -231,6 +232,10 @@ pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t)
         }
         if (t->max_speculation) c.tune.max_spec = t->max_speculation;
         if (t->use_graphs) c.tune.use_graphs = t->use_graphs == 1u ? 1u : 0u;
+        if (t->plain_launch) {
+            if (t->plain_launch != 1u && t->plain_launch != 2u) throw Error(PCS_ERR_INVALID_ARGUMENT, "plain_launch must be 1 or 2");
+            c.tune.plain_launch = t->plain_launch;
+        }
         c.graph_dirty = true;
     });
 }

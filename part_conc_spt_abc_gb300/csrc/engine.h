@@ -58,6 +58,7 @@ struct Tuning {
     uint32_t capacity = 2048;
     uint32_t max_spec = 4096;
     uint32_t use_graphs = 1;
+    uint32_t plain_launch = 1; /* 1 reference geometry, 2 persistent grid */
 };
 
 struct Job;

@@ -13,7 +13,7 @@
  *
  *   k_round_plan   shares the round's proposal capacity among the jobs
  *                  (trials per pending slot k = capacity / pending, clamped)
- *   k_propose      one thread per proposal: parent pick, perturbation,
+ *   k_propose      one warp per proposal: parent pick, perturbation,
  *                  label sort, per-proposal forward-model arguments, Poisson
  *                  counts per video (transformed rejection, Hoermann 1993)
  *   k_items        scan of work items and the item -> proposal map
@@ -106,11 +106,18 @@ __global__ void k_round_plan(PmcArgs a)
 }
 
 /* ----------------------------------------------------------------------- */
-__global__ void __launch_bounds__(128) k_propose(PmcArgs a)
+/* one warp per proposal: lane 0 builds the parameters and forward-model
+ * arguments (FP64), the lanes draw the per-video Poisson counts in parallel
+ * (each count has its own Philox counter, so the counts equal
+ * pcs_draw_counts') and scan them into the video prefix. */
+constexpr uint32_t kProposeWarps = 8;
+
+__global__ void __launch_bounds__(32 * kProposeWarps) k_propose(PmcArgs a)
 {
     RoundDev* rd = a.round;
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= rd->n_props) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t q = blockIdx.x * kProposeWarps + (threadIdx.x >> 5);
+    if (q >= rd->n_props) return; /* whole warp */
     const uint32_t j = job_of_(rd, q);
     JobPmcDev& pm = a.pmc[j];
     const JobDev& jd = a.jobs[j];
@@ -122,23 +129,48 @@ __global__ void __launch_bounds__(128) k_propose(PmcArgs a)
     const uint32_t gen = pm.generation;
     const uint32_t k0 = jd.seed_lo, k1 = jd.seed_hi;
 
-    double th[PCS_MAX_P];
-    pcs_build_theta(pm, pm.theta, pm.wcum, pm.factor, slot, trial, gen, k0, k1, th);
-    double* out = a.theta_prop + (uint64_t)q * PCS_MAX_P;
-    for (uint32_t p = 0; p < pm.P; ++p) out[p] = th[p];
-
     PropDev pd;
-    pd.job = j;
-    pd.slot = slot;
-    pd.trial = trial;
-    pd.gen = gen;
-    pd.quirk_full_az = 0u;
-    const double lambda = pcs_build_args(pm, th, gen, pd);
+    double lambda = 0.0;
+    if (lane == 0u) {
+        double th[PCS_MAX_P];
+        pcs_build_theta(pm, pm.theta, pm.wcum, pm.factor, slot, trial, gen, k0, k1, th);
+        double* out = a.theta_prop + (uint64_t)q * PCS_MAX_P;
+        for (uint32_t p = 0; p < pm.P; ++p) out[p] = th[p];
+        pd.job = j;
+        pd.slot = slot;
+        pd.trial = trial;
+        pd.gen = gen;
+        pd.quirk_full_az = 0u;
+        lambda = pcs_build_args(pm, th, gen, pd);
+    }
+    lambda = __shfl_sync(0xFFFFFFFFu, lambda, 0);
 
     const uint64_t coff = (uint64_t)q * (2u * rd->v_max + 1u);
     uint32_t* cnt = a.counts + coff;
-    uint64_t steps = 0;
-    const uint64_t total = pcs_draw_counts(lambda, jd.V, jd.frames, slot, trial, gen, k0, k1, cnt, cnt + jd.V, &steps);
+    uint32_t* pre = cnt + jd.V;
+    const uint32_t gt = pcs_ctr_gen_trial(gen, trial);
+    uint64_t run = 0, steps = 0;
+    if (lane == 0u) pre[0] = 0u;
+    for (uint32_t v0 = 0; v0 < jd.V; v0 += 32u) {
+        const uint32_t v = v0 + lane;
+        uint32_t c = 0u;
+        if (v < jd.V) {
+            c = pcs_poisson(lambda, v, slot, gt, k0, k1);
+            cnt[v] = c;
+            steps += (uint64_t)c * jd.frames[v];
+        }
+        uint64_t incl = c;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint64_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if ((int)lane >= d) incl += t;
+        }
+        const uint64_t tot = run + incl;
+        if (v < jd.V) pre[v + 1] = (uint32_t)(tot < 0xFFFFFFFFull ? tot : 0xFFFFFFFFull);
+        run += __shfl_sync(0xFFFFFFFFu, incl, 31);
+    }
+    for (int d = 16; d >= 1; d >>= 1) steps += __shfl_xor_sync(0xFFFFFFFFu, steps, d);
+    if (lane != 0u) return;
+    const uint64_t total = run;
     if (total > 0xFFFFFFFFull) atomicOr(a.err, PCS_ERRBIT_COUNTS);
     pd.total_particles = (uint32_t)min(total, (uint64_t)0xFFFFFFFFu);
     pd.counts_off = coff;
@@ -631,7 +663,7 @@ cudaError_t launch_round_plan(const PmcArgs& a, cudaStream_t st)
 
 cudaError_t launch_propose(const PmcArgs& a, uint32_t capacity, cudaStream_t st)
 {
-    k_propose<<<(capacity + 127) / 128, 128, 0, st>>>(a);
+    k_propose<<<(capacity + kProposeWarps - 1) / kProposeWarps, 32 * kProposeWarps, 0, st>>>(a);
     return cudaGetLastError();
 }
 

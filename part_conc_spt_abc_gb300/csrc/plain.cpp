@@ -74,7 +74,12 @@ void run_plain(Job& j, uint32_t max_steps, uint32_t queues)
     /* particles per proposal are bounded by the prior's largest Poisson mean */
     const double lam_max = (double)j.C * j.p.ub_c * j.p.Lx * j.p.Ly * j.p.Lz / 1e12;
     const uint64_t parts_max = (uint64_t)std::ceil((lam_max + 12.0 * std::sqrt(lam_max) + 16.0) * V);
-    const uint32_t items_cap = (uint32_t)std::min<uint64_t>(parts_max / c.tune.chunk + 2, 1u << 30);
+    /* launch geometry: the reference's (ceil(V/4) CTAs of 128 threads per
+     * proposal, simulation_impl.inl:655-656, launched at :1065), or this
+     * build's full persistent grid */
+    const bool ref_geometry = c.tune.plain_launch != 2u;
+    const uint32_t chunk = ref_geometry ? 128u : c.tune.chunk;
+    const uint32_t items_cap = (uint32_t)std::min<uint64_t>(parts_max / chunk + 2, 1u << 30);
     std::vector<Queue> qs(queues);
     for (auto& q : qs) {
         PCS_CUDA(cudaStreamCreateWithFlags(&q.st, cudaStreamNonBlocking));
@@ -109,11 +114,11 @@ void run_plain(Job& j, uint32_t max_steps, uint32_t queues)
 
     const uint32_t tile_words = tile_words_for(std::min<uint32_t>(c.tune.tile_rows, j.R), j.B);
     SimLaunch sl{};
-    sl.block = c.tune.block;
-    sl.ppt = (int)c.tune.ppt;
+    sl.block = ref_geometry ? 128u : c.tune.block;
+    sl.ppt = ref_geometry ? 1 : (int)c.tune.ppt;
     sl.replay = false;
     sl.aggregate = c.tune.aggregate == 1u;
-    const uint32_t sim_slots = c.sim_grid(sl.block, c.tune.ppt, sl.aggregate, tile_words);
+    const uint32_t sim_slots = ref_geometry ? (V + 3u) / 4u : c.sim_grid(sl.block, c.tune.ppt, sl.aggregate, tile_words);
 
     JobPmcDev st = j.status; /* counters reported through pcs_job_info */
     uint64_t gen_trials = 0;
@@ -136,7 +141,7 @@ void run_plain(Job& j, uint32_t max_steps, uint32_t queues)
         pd.counts_off = 0;
         pd.hist_off = 0;
         pd.item_begin = 0;
-        pd.item_count = (uint32_t)((total + c.tune.chunk - 1) / c.tune.chunk);
+        pd.item_count = (uint32_t)((total + chunk - 1) / chunk);
         if (pd.item_count > items_cap) throw Error(PCS_ERR_DEVICE, "work items exceed the plain-form capacity");
         q.h_ctl[0] = pd.item_count;
         q.h_ctl[1] = 0u;
@@ -151,11 +156,11 @@ void run_plain(Job& j, uint32_t max_steps, uint32_t queues)
         a.item_prop = q.d_items.as<uint32_t>();
         a.n_items = q.d_ctl.as<uint32_t>();
         a.queue_head = q.d_ctl.as<uint32_t>() + 1;
-        a.chunk = c.tune.chunk;
+        a.chunk = chunk;
         a.tile_words = tile_words;
         a.err = c.err.as<uint32_t>();
         SimLaunch l = sl;
-        l.grid = std::max<uint32_t>(1u, std::min<uint32_t>(pd.item_count, sim_slots));
+        l.grid = ref_geometry ? sim_slots : std::max<uint32_t>(1u, std::min<uint32_t>(pd.item_count, sim_slots));
         PCS_CUDA(launch_simulate(a, l, q.st));
         DistArgs d{};
         d.jobs = d_job.as<JobDev>();

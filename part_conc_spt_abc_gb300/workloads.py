@@ -10,6 +10,9 @@ cumulative histogram is exactly the simulated one.
            frames, pop 256, epsilon = 50% quantile, 8 generations
   config1  2 components 175/500 nm (sd 10/25, weights 0.6/0.4), 5e14 m^-3,
            50 videos x 300 frames, R x B = 301 x 128, pop 1024, 12 generations
+  config2  2 components U(100,800) nm, concentration prior spanning a mean
+           of 50..5000 particles per video, 20 videos x 200 frames, 201 x 100
+           bins, pop 512 (one 512-proposal round per launch)
   config3  3 components 100/250/600 nm (sd 5%, weights 0.3/0.4/0.3), 1e5
            particles per video, 100 videos x 1000 frames, 1001 x 256 bins,
            pop 4096, 10 generations
@@ -125,10 +128,27 @@ def config1(ctx, seed=0, generations=12):
     return make_problem(ctx, [175.0, 500.0], [10.0, 25.0], 5e14, [0.6, 0.4], 50, 300, 128, 1024, generations, seed)
 
 
+def config2(ctx, seed=0, generations=8):
+    """512-proposal rounds with uneven Poisson means: two components with
+    diameters drawn U(100, 800) nm, concentration prior spanning a mean of
+    50..5000 particles per video (each component 25..2500), 20 videos x 200
+    frames, 201 x 100 bins, population 512."""
+    rng = np.random.default_rng(1000 + seed)
+    mu = sorted(rng.uniform(100.0, 800.0, 2).tolist())
+    vol_ml = BOX[0] * BOX[1] * BOX[2] / 1e12
+    lam_to_m3 = 1e6 / vol_ml
+    return make_problem(ctx, mu, [0.05 * m for m in mu], 1000.0 * lam_to_m3, [0.5, 0.5], 20, 200, 100, 512,
+                        generations, seed, prior_mu=(100.0, 800.0), prior_sd=(1.0, 100.0),
+                        prior_conc_m3=(25.0 * lam_to_m3, 2500.0 * lam_to_m3))
+
+
 def config3(ctx, seed=0, generations=10):
+    """1e5 particles per video in total; each component's concentration prior
+    spans 1e4..1e5 particles per video, so prior-pass proposals average about
+    1.2e5 particles per video (1.2e10 particle-steps each)."""
     conc = 1e5 / (BOX[0] * BOX[1] * BOX[2] / 1e12) * 1e6
     return make_problem(ctx, [100.0, 250.0, 600.0], [5.0, 12.5, 30.0], conc, [0.3, 0.4, 0.3], 100, 1000, 256,
-                        4096, generations, seed, prior_conc_m3=(conc / 10, conc * 10))
+                        4096, generations, seed, prior_conc_m3=(conc / 10, conc))
 
 
 def serve_stream(ctx, n_jobs=64, seed=0, rate_per_s=2.0, pop_range=(256, 4096), gen_range=(6, 12),
