@@ -292,6 +292,29 @@ def run_serve(args, rank, world):
     ctx.close()
 
 
+def run_plain_config(args, P, ctx, inp, workload, rank):
+    """The plain form (reference schedule, 30 queues) on one configuration:
+    prior pass plus --steps generations, wall-clock timed (host PMC)."""
+    ctx.set_tuning(plain_launch=args.plain)
+    inp.params.max_generations = args.steps
+    sim = P.make_simulation(ctx, inp, seed=1 + rank)
+    t0 = time.perf_counter()
+    sim.run_plain(0, 30)
+    dt = time.perf_counter() - t0
+    inf = sim.info()
+    sim.close()
+    line = {"impl": "plain", "metric": "particle-steps/s", "value": inf.particle_steps / dt,
+            "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": 0,
+            "ms_per_step": 1e3 * dt / (args.steps + 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload, "step": "prior pass + generations, reference per-proposal schedule",
+                       "plain_launch": {1: "reference ceil(V/4) x 128", 2: "persistent grid"}[args.plain]},
+            "proposals_per_s": inf.simulations / dt, "accepted_per_s": inf.accepted / dt, "wall_s": dt}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -301,6 +324,9 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="configuration 0 (pop 256): the case profiled under ncu")
+    ap.add_argument("--plain", type=int, default=0, choices=[0, 1, 2],
+                    help="time the plain form instead (1: reference launch geometry, 2: persistent grid) "
+                         "over --steps generations")
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3],
                     help="benchmark configuration (1 is the headline; 3 times a fixed 64-proposal slice)")
     ap.add_argument("--serve", action="store_true", help="the 64-job serving stream, served vs plain")
@@ -339,6 +365,10 @@ def main():
     tune = dict(block=t.block_size, ppt=t.particles_per_thread, tile_rows=t.hist_tile_rows,
                 warp_aggregate=t.warp_aggregate, chunk=t.chunk_particles, capacity=t.round_capacity,
                 autotuned=not args.no_autotune and cfg != 3)
+
+    if args.plain:
+        run_plain_config(args, P, ctx, inp, workload, rank)
+        return
 
     def stepper(sim):
         """advance one step: a generation, or one round of the fixed slice"""

@@ -133,7 +133,7 @@ size_t pcs_device_report(char* buf, size_t cap);
 
 /* Tuning knobs.  In pcs_set_tuning a field of 0 keeps the current /
  * autotuned value; PCS_TUNE_ZERO sets a field to 0 where 0 is meaningful
- * (hist_tile_rows, warp_aggregate, use_graphs).  pcs_get_tuning reports
+ * (hist_tile_rows, warp_aggregate, use_graphs, round_fill).  pcs_get_tuning reports
  * plain values. */
 #define PCS_TUNE_ZERO 0xFFFFFFFFu
 typedef struct pcs_tuning {
@@ -148,6 +148,9 @@ typedef struct pcs_tuning {
     uint32_t plain_launch;        /* pcs_job_run_plain's simulate launch: 1 the reference's
                                    * geometry (ceil(V/4) CTAs x 128 threads per proposal,
                                    * default), 2 this build's persistent grid */
+    uint32_t round_fill;          /* a round with fewer proposals than this (the end of a
+                                   * generation) gives its pending slots extra trials, up to
+                                   * the capacity; default 1024, PCS_TUNE_ZERO: none */
 } pcs_tuning;
 pcs_status pcs_get_tuning(pcs_ctx* ctx, pcs_tuning* out);
 pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t);

@@ -60,6 +60,7 @@ class Tuning(C.Structure):
         ("block_size", C.c_uint32), ("particles_per_thread", C.c_uint32), ("hist_tile_rows", C.c_uint32),
         ("warp_aggregate", C.c_uint32), ("chunk_particles", C.c_uint32), ("round_capacity", C.c_uint32),
         ("max_speculation", C.c_uint32), ("use_graphs", C.c_uint32), ("plain_launch", C.c_uint32),
+        ("round_fill", C.c_uint32),
     ]
 
 

@@ -205,6 +205,7 @@ pcs_status pcs_get_tuning(pcs_ctx* ctx, pcs_tuning* out)
         out->max_speculation = c.tune.max_spec;
         out->use_graphs = c.tune.use_graphs;
         out->plain_launch = c.tune.plain_launch;
+        out->round_fill = c.tune.round_fill;
     });
 }
 
@@ -236,6 +237,7 @@ pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t)
             if (t->plain_launch != 1u && t->plain_launch != 2u) throw Error(PCS_ERR_INVALID_ARGUMENT, "plain_launch must be 1 or 2");
             c.tune.plain_launch = t->plain_launch;
         }
+        if (t->round_fill) c.tune.round_fill = t->round_fill == 0xFFFFFFFFu ? 0u : t->round_fill;
         c.graph_dirty = true;
     });
 }

@@ -511,6 +511,7 @@ void Ctx::upload_table()
     r.n_jobs = n;
     r.capacity = rb.capacity;
     r.max_spec = tune.max_spec;
+    r.fill = std::min(tune.round_fill, rb.capacity);
     r.chunk = tune.chunk;
     r.items_cap = rb.items_cap;
     r.counts_cap = rb.counts_cap;

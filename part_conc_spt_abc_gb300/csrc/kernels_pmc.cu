@@ -67,13 +67,15 @@ __global__ void k_round_plan(PmcArgs a)
     uint32_t k = total_pending ? (uint32_t)(rd->capacity / total_pending) : 1u;
     if (k < 1u) k = 1u;
     if (k > rd->max_spec) k = rd->max_spec;
-    uint32_t base = 0;
-    uint64_t hbase = 0;
-    for (uint32_t j = 0; j < rd->n_jobs; ++j) {
+    /* trials per pending slot: enough to fill the round, but not many more
+     * than ~0.3 / (acceptance rate so far), so that few trials are simulated
+     * after a slot's first acceptance -- unless that leaves the round below
+     * `fill` proposals (the end of a generation, when few slots are left and
+     * the GPU would idle), in which case the slots get more trials, up to k */
+    uint32_t kjs[kMaxRoundJobs];
+    uint64_t want_total = 0, pend_spec = 0;
+    for (uint32_t j = 0; j < rd->n_jobs && j < kMaxRoundJobs; ++j) {
         const JobPmcDev& pm = a.pmc[j];
-        /* trials per pending slot: enough to fill the round, but not many
-         * more than ~0.3 / (acceptance rate so far), so that few trials
-         * are simulated after a slot's first acceptance */
         uint32_t kj = k;
         if (pm.generation == 0u) {
             kj = 1u; /* prior pass: one simulation per slot */
@@ -81,7 +83,21 @@ __global__ void k_round_plan(PmcArgs a)
             const double pacc = ((double)pm.accepted_gen + 1.0) / ((double)pm.trials + 2.0);
             const double kw = ceil(0.3 / pacc);
             if (kw < (double)kj) kj = (uint32_t)(kw < 1.0 ? 1.0 : kw);
+            if (!pm.done) pend_spec += pm.pending_count;
         }
+        kjs[j] = kj;
+        if (!pm.done) want_total += (uint64_t)pm.pending_count * kj;
+    }
+    if (want_total < rd->fill && pend_spec > 0) {
+        const uint64_t kf = (rd->fill - want_total + pend_spec - 1) / pend_spec;
+        for (uint32_t j = 0; j < rd->n_jobs && j < kMaxRoundJobs; ++j)
+            if (a.pmc[j].generation > 0u) kjs[j] = (uint32_t)min((uint64_t)k, (uint64_t)kjs[j] + kf);
+    }
+    uint32_t base = 0;
+    uint64_t hbase = 0;
+    for (uint32_t j = 0; j < rd->n_jobs; ++j) {
+        const JobPmcDev& pm = a.pmc[j];
+        const uint32_t kj = j < kMaxRoundJobs ? kjs[j] : 1u;
         uint64_t want = pm.done ? 0u : (uint64_t)pm.pending_count * kj;
         uint64_t room = rd->capacity - base;
         const uint64_t rb = (uint64_t)a.jobs[j].R * a.jobs[j].B;

@@ -16,8 +16,10 @@
  * order, so given the same draws the histogram is bit-exact with the
  * reference kernel built without FMA contraction.
  *
- * Random draws: Philox4x32-10 keyed by the job seed, counter
- * (particle, tag|block, slot, generation|trial); block 0 = position and
+ * Random draws: Philox4x32-10, counter (particle, tag|block, slot,
+ * generation|trial) with the job seed folded into words 2 and 3; the rounds'
+ * work on the words that stay fixed for a particle is done once per particle
+ * (pcs_philox_prepare); block 0 = position and
  * component, block 1 = size, blocks 2+3g..4+3g = the 12 normals of walk steps
  * 4g+1..4g+4 (Box-Muller on word pairs).  In replay mode the same kernel
  * reads pre-generated draws instead.
@@ -52,7 +54,8 @@ __device__ __forceinline__ void box_muller_(uint32_t ra, uint32_t rb, float& n0,
 
 struct Walker {
     float x, y, z, de, sd, haz;
-    uint32_t k, F, n; /* n: particle index within the proposal */
+    uint32_t k, F, n;  /* n: particle index within the proposal */
+    pcs_philox_pre ph; /* the particle's stream with its fixed counter words folded in */
 };
 
 struct ItemCtx {
@@ -233,7 +236,8 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
                         u2 = u[2];
                         u3 = u[3];
                     } else {
-                        pcs_u4 r = pcs_draw(n, pcs_ctr_tag(PCS_STREAM_PARTICLE, 0u), slot, gt, k0, k1);
+                        q.ph = pcs_philox_prepare(n, slot, gt, k0, k1);
+                        pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 0u));
                         u0 = pcs_u01_24(r.x);
                         u1 = pcs_u01_24(r.y);
                         u2 = pcs_u01_24(r.z);
@@ -253,7 +257,7 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
                         if (REPLAY) {
                             q.sd = a.rp_sigmas[n];
                         } else {
-                            pcs_u4 r = pcs_draw(n, pcs_ctr_tag(PCS_STREAM_PARTICLE, 1u), slot, gt, k0, k1);
+                            pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 1u));
                             float z0, z1;
                             box_muller_(r.x, r.y, z0, z1);
                             q.sd = s_prop.sd_scale[comp] * expf(s_prop.sd_shape[comp] * z0);
@@ -283,7 +287,7 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
                     } else {
 #pragma unroll
                         for (int b = 0; b < 3; ++b) {
-                            pcs_u4 r = pcs_draw(q.n, pcs_ctr_tag(PCS_STREAM_PARTICLE, 2u + 3u * g + (uint32_t)b), slot, gt, k0, k1);
+                            pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 2u + 3u * g + (uint32_t)b));
                             box_muller_(r.x, r.y, nn[4 * b + 0], nn[4 * b + 1]);
                             box_muller_(r.z, r.w, nn[4 * b + 2], nn[4 * b + 3]);
                         }

@@ -69,7 +69,8 @@ def test_results_do_not_depend_on_batching(pcs, ctx):
     settings = [dict(max_speculation=1), dict(max_speculation=3, block_size=128, particles_per_thread=2),
                 dict(round_capacity=200, max_speculation=64),
                 dict(max_speculation=4096, block_size=512, particles_per_thread=4, hist_tile_rows=8,
-                     warp_aggregate=1)]
+                     warp_aggregate=1),
+                dict(round_fill=0xFFFFFFFF), dict(round_fill=2000)]
     try:
         for kw in settings:
             ctx.set_tuning(**kw)
@@ -80,7 +81,7 @@ def test_results_do_not_depend_on_batching(pcs, ctx):
             assert info.gamma == ref_info.gamma
     finally:
         ctx.set_tuning(max_speculation=4096, block_size=256, particles_per_thread=1, hist_tile_rows=64,
-                       warp_aggregate=0xFFFFFFFF, round_capacity=2048)
+                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=1024)
 
 
 @pytest.mark.parametrize("plain_launch", [1, 2], ids=["reference_launch", "persistent_grid"])
