@@ -150,7 +150,8 @@ typedef struct pcs_tuning {
                                    * default), 2 this build's persistent grid */
     uint32_t round_fill;          /* a round with fewer proposals than this (the end of a
                                    * generation) gives its pending slots extra trials, up to
-                                   * the capacity; default 1024, PCS_TUNE_ZERO: none */
+                                   * the capacity; default none.  It raises proposals/s at the
+                                   * ends of generations but adds trials after acceptances */
 } pcs_tuning;
 pcs_status pcs_get_tuning(pcs_ctx* ctx, pcs_tuning* out);
 pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t);

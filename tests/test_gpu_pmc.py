@@ -81,7 +81,7 @@ def test_results_do_not_depend_on_batching(pcs, ctx):
             assert info.gamma == ref_info.gamma
     finally:
         ctx.set_tuning(max_speculation=4096, block_size=256, particles_per_thread=1, hist_tile_rows=64,
-                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=1024)
+                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=0xFFFFFFFF)
 
 
 @pytest.mark.parametrize("plain_launch", [1, 2], ids=["reference_launch", "persistent_grid"])
