@@ -336,10 +336,10 @@ pcs_status pcs_scan_distance(pcs_ctx* ctx, const uint32_t* hist, const uint32_t*
                              float* dist_f32, double* dist_f64, uint64_t* ssd);
 
 /* pcs_scan_distance for callers that cannot allocate device memory; this
- * entry point has no counterpart in the reference.  Callers capturing a CUDA
- * graph, hosts whose own caching allocator owns all device memory, and
- * real-time loops where an allocation could stall on device synchronisation
- * cannot let a library call cudaMalloc; this variant takes device pointers
+ * entry point has no counterpart in the reference.  Hosts whose own caching
+ * allocator owns all device memory, services under a fixed device-memory
+ * budget, and real-time loops where an allocation could stall on device
+ * synchronisation cannot let a library call cudaMalloc; this variant takes device pointers
  * and keeps its working buffers (the transposed observed histogram and one
  * descriptor per histogram) in a fixed __device__ array instead, calling no
  * allocator.  d_hist holds count x rows x bins counts and is reset to zero,

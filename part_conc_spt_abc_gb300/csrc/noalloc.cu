@@ -5,10 +5,10 @@
  * pcs_scan_distance stages its inputs and its working buffers (the observed
  * cumulative histogram transposed for coalesced column sweeps, one
  * descriptor per histogram, a proposal counter) in memory it allocates per
- * call.  Some callers cannot let a library call cudaMalloc: code running
- * while a CUDA graph is being captured, a host framework whose caching
- * allocator owns all device memory and must not be bypassed, or a real-time
- * loop where an allocation may block on device synchronisation.  This entry
+ * call.  Some callers cannot let a library call cudaMalloc: a host
+ * framework whose caching allocator owns all device memory and must not be
+ * bypassed, a service running under a fixed device-memory budget, or a
+ * real-time loop where an allocation may block on device synchronisation.  This entry
  * point takes device pointers for its inputs and outputs and keeps its
  * working buffers in one file-scope __device__ array of fixed size, so it
  * allocates nothing.

@@ -1,6 +1,6 @@
 """pcs_scan_distance_noalloc: the distance kernel for callers that cannot
-let a library allocate device memory (graph capture, a host framework's own
-caching allocator, real-time loops).  It must give exactly what
+let a library allocate device memory (a host framework's own caching
+allocator, a fixed device-memory budget, real-time loops).  It must give exactly what
 pcs_scan_distance gives, reset the histograms it consumed, refuse sizes
 beyond its fixed scratch, and work on back-to-back calls that reuse the
 shared scratch.  Buffers here come from torch, i.e. from the caller."""
