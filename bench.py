@@ -329,6 +329,8 @@ def main():
     ap.add_argument("--plain", type=int, default=0, choices=[0, 1, 2],
                     help="time the plain form instead (1: reference launch geometry, 2: persistent grid) "
                          "over --steps generations")
+    ap.add_argument("--no-round-fill", action="store_true",
+                    help="no extra trials for rounds that would underfill the GPU")
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3],
                     help="benchmark configuration (1 is the headline; 3 times a fixed 64-proposal slice)")
     ap.add_argument("--serve", action="store_true", help="the 64-job serving stream, served vs plain")
@@ -359,12 +361,14 @@ def main():
     inp, truth = {0: W.config0, 1: W.config1, 2: W.config2, 3: W.config3}[cfg](ctx, seed=0, generations=gens)
     if not args.no_autotune and cfg != 3:
         ctx.autotune(inp)
+    if args.no_round_fill:
+        ctx.set_tuning(round_fill=0xFFFFFFFF)
     if cfg == 2:
         ctx.set_tuning(round_capacity=512)
     if cfg == 3:
         ctx.set_tuning(round_capacity=64)
     t = ctx.tuning
-    tune = dict(block=t.block_size, ppt=t.particles_per_thread, tile_rows=t.hist_tile_rows,
+    tune = dict(round_fill=t.round_fill, block=t.block_size, ppt=t.particles_per_thread, tile_rows=t.hist_tile_rows,
                 warp_aggregate=t.warp_aggregate, chunk=t.chunk_particles, capacity=t.round_capacity,
                 autotuned=not args.no_autotune and cfg != 3)
 

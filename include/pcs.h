@@ -148,10 +148,11 @@ typedef struct pcs_tuning {
     uint32_t plain_launch;        /* pcs_job_run_plain's simulate launch: 1 the reference's
                                    * geometry (ceil(V/4) CTAs x 128 threads per proposal,
                                    * default), 2 this build's persistent grid */
-    uint32_t round_fill;          /* a round with fewer proposals than this (the end of a
-                                   * generation) gives its pending slots extra trials, up to
-                                   * the capacity; default none.  It raises proposals/s at the
-                                   * ends of generations but adds trials after acceptances */
+    uint32_t round_fill;          /* a round whose proposals would carry fewer particles than
+                                   * this (the end of a generation) gives its pending slots
+                                   * proportionally more trials, up to the capacity.  Default:
+                                   * one wave of the simulate launch (SMs x 2048 threads);
+                                   * PCS_TUNE_ZERO: none */
 } pcs_tuning;
 pcs_status pcs_get_tuning(pcs_ctx* ctx, pcs_tuning* out);
 pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t);

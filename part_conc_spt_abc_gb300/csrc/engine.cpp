@@ -401,6 +401,7 @@ Ctx::Ctx(int dev, int infl) : device(dev), inflight(infl > 0 ? infl : 1)
     if (dev < 0 || dev >= n) throw Error(PCS_ERR_INVALID_ARGUMENT, "no CUDA device " + std::to_string(dev));
     PCS_CUDA(cudaSetDevice(dev));
     PCS_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
+    tune.round_fill = (uint32_t)sm_count * 2048u; /* one full-occupancy wave of walkers */
     PCS_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     err.alloc(16);
     PCS_CUDA(cudaMemset(err.p, 0, 16));
@@ -511,7 +512,7 @@ void Ctx::upload_table()
     r.n_jobs = n;
     r.capacity = rb.capacity;
     r.max_spec = tune.max_spec;
-    r.fill = std::min(tune.round_fill, rb.capacity);
+    r.fill = tune.round_fill;
     r.chunk = tune.chunk;
     r.items_cap = rb.items_cap;
     r.counts_cap = rb.counts_cap;

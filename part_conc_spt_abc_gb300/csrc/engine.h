@@ -59,7 +59,7 @@ struct Tuning {
     uint32_t max_spec = 4096;
     uint32_t use_graphs = 1;
     uint32_t plain_launch = 1; /* 1 reference geometry, 2 persistent grid */
-    uint32_t round_fill = 0; /* proposals a round is topped up to (0: no top-up) */
+    uint32_t round_fill = 0; /* particles a round is topped up to (0: none); set to one wave at open */
 };
 
 struct Job;

@@ -69,11 +69,14 @@ __global__ void k_round_plan(PmcArgs a)
     if (k > rd->max_spec) k = rd->max_spec;
     /* trials per pending slot: enough to fill the round, but not many more
      * than ~0.3 / (acceptance rate so far), so that few trials are simulated
-     * after a slot's first acceptance -- unless that leaves the round below
-     * `fill` proposals (the end of a generation, when few slots are left and
-     * the GPU would idle), in which case the slots get more trials, up to k */
+     * after a slot's first acceptance -- unless the round's proposals would
+     * then carry fewer than `fill` particles (one wave of the simulate
+     * launch; at the end of a generation few slots are left and the GPU
+     * would idle), in which case the slots get proportionally more trials,
+     * up to k.  Particles per proposal are estimated from the job's history. */
     uint32_t kjs[kMaxRoundJobs];
-    uint64_t want_total = 0, pend_spec = 0;
+    double planned = 0.0;
+    uint64_t pend_spec = 0;
     for (uint32_t j = 0; j < rd->n_jobs && j < kMaxRoundJobs; ++j) {
         const JobPmcDev& pm = a.pmc[j];
         uint32_t kj = k;
@@ -86,12 +89,19 @@ __global__ void k_round_plan(PmcArgs a)
             if (!pm.done) pend_spec += pm.pending_count;
         }
         kjs[j] = kj;
-        if (!pm.done) want_total += (uint64_t)pm.pending_count * kj;
+        if (!pm.done) {
+            /* particles per proposal so far (steps over the longest video) */
+            const double ppp = pm.simulations ? (double)pm.particle_steps / (double)pm.simulations /
+                                                    (double)max(a.jobs[j].frames_max, 1u)
+                                              : (double)rd->fill;
+            planned += (double)pm.pending_count * kj * ppp;
+        }
     }
-    if (want_total < rd->fill && pend_spec > 0) {
-        const uint64_t kf = (rd->fill - want_total + pend_spec - 1) / pend_spec;
+    if (rd->fill && planned < (double)rd->fill && pend_spec > 0) {
+        const double f = planned > 0.0 ? (double)rd->fill / planned : (double)k;
         for (uint32_t j = 0; j < rd->n_jobs && j < kMaxRoundJobs; ++j)
-            if (a.pmc[j].generation > 0u) kjs[j] = (uint32_t)min((uint64_t)k, (uint64_t)kjs[j] + kf);
+            if (a.pmc[j].generation > 0u && !a.pmc[j].done)
+                kjs[j] = (uint32_t)min((double)k, fmax((double)kjs[j], ceil((double)kjs[j] * f)));
     }
     uint32_t base = 0;
     uint64_t hbase = 0;

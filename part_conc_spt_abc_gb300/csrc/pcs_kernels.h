@@ -120,7 +120,7 @@ struct RoundDev {
     uint64_t counts_cap;      /* u32 words */
     uint64_t hist_cap;        /* u32 words */
     uint32_t v_max;           /* counts stride = 2 * v_max + 1 per proposal */
-    uint32_t fill;            /* proposals a round is topped up to with extra trials */
+    uint32_t fill;            /* particles a round is topped up to with extra trials (0: none) */
     /* device-written */
     uint32_t n_props;
     uint32_t n_items;

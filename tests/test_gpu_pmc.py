@@ -65,12 +65,13 @@ def test_generation_invariants(pcs, ctx):
 
 def test_results_do_not_depend_on_batching(pcs, ctx):
     inp, _ = small_input(pcs, C=1, pop=64)
+    fill0 = ctx.tuning.round_fill
     ref_out, ref_info = run_job(pcs, ctx, inp, 9, 3)
     settings = [dict(max_speculation=1), dict(max_speculation=3, block_size=128, particles_per_thread=2),
                 dict(round_capacity=200, max_speculation=64),
                 dict(max_speculation=4096, block_size=512, particles_per_thread=4, hist_tile_rows=8,
                      warp_aggregate=1),
-                dict(round_fill=0xFFFFFFFF), dict(round_fill=2000)]
+                dict(round_fill=0xFFFFFFFF), dict(round_fill=3000000)]
     try:
         for kw in settings:
             ctx.set_tuning(**kw)
@@ -81,7 +82,7 @@ def test_results_do_not_depend_on_batching(pcs, ctx):
             assert info.gamma == ref_info.gamma
     finally:
         ctx.set_tuning(max_speculation=4096, block_size=256, particles_per_thread=1, hist_tile_rows=64,
-                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=0xFFFFFFFF)
+                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=fill0)
 
 
 @pytest.mark.parametrize("plain_launch", [1, 2], ids=["reference_launch", "persistent_grid"])
