@@ -294,6 +294,20 @@ def run_serve(args, rank, world):
     ctx.close()
 
 
+def simulate_traffic(launch_ms: float):
+    """DRAM bytes (read + write) of one k_simulate launch, from the ncu
+    capture of a configuration-1 launch summarised in profiles/ (line
+    'dram bytes per ms of launch: X'), scaled to this run's mean launch
+    time; None when the summary is absent."""
+    import re
+    try:
+        with open(os.path.join(ROOT, "profiles", "k_simulate_config1_ncu_full.md")) as f:
+            m = re.search(r"dram bytes per ms of launch:\s*([0-9.eE+]+)", f.read())
+    except OSError:
+        return None
+    return float(m.group(1)) * launch_ms if m else None
+
+
 def run_plain_config(args, P, ctx, inp, workload, rank):
     """The plain form (reference schedule, 30 queues) on one configuration:
     prior pass plus --steps generations, wall-clock timed (host PMC)."""
@@ -433,13 +447,7 @@ def main():
     achieved = steps_per_launch * OPS_PER_STEP / (sim_ms / 1e3) / 1e12
     sm_count = device_sm_count(P, local)
     peak = sm_count * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "simulate_config1_traffic.json")
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("bytes_per_launch")
-        except (OSError, ValueError):
-            traffic = None
+    traffic = simulate_traffic(sim_ms) if cfg == 1 else None
     dist_ms = ks.distance_ms / max(1, ks.distance_launches)
     dist_gbs = (ks.histogram_cells / max(1, ks.distance_launches)) * DIST_BYTES_PER_CELL / (dist_ms / 1e3) / 1e9
 
