@@ -223,6 +223,19 @@ pcs_status pcs_job_info_get(pcs_job* job, pcs_job_info* out);
 pcs_status pcs_job_output(pcs_job* job, double* m, double* s, double* c, double* az,
                           double* dist, double* w);
 
+/* Checkpoint / resume (no counterpart in the reference).  Between any two
+ * API calls a job's state is complete on the host side of a round; since
+ * every draw is keyed by (seed, generation, slot, trial), a job restored from
+ * a checkpoint continues exactly as the original would have.
+ * pcs_job_checkpoint: with buf NULL, *bytes receives the size; otherwise the
+ * state is written to buf (cap >= that size).  The job must have run at
+ * least one round.  pcs_job_restore loads a checkpoint into a job that has
+ * not run yet and was created with the same parameters shape (N, P, C, Z,
+ * V, R, B, model), observed data and seed; its own max_generations applies
+ * from then on.  Plain-form runs (pcs_job_run_plain) are not checkpointed. */
+pcs_status pcs_job_checkpoint(pcs_job* job, void* buf, size_t cap, size_t* bytes);
+pcs_status pcs_job_restore(pcs_job* job, const void* buf, size_t bytes);
+
 /* ------------------------------------------------------------------ */
 /* Serving: continuous batching of independent jobs                    */
 /* ------------------------------------------------------------------ */

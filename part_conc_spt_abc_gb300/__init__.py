@@ -244,6 +244,20 @@ class Simulation:
         return Output(p.model, p.weighting_scheme, N, Cc, Z, m, c, az, d, w, bool(i.converged), i.gamma,
                       s if p.model == MODEL_LOGNORMAL else None, meta)
 
+    def checkpoint(self) -> bytes:
+        """The job's state after its last round (exact resume point)."""
+        n = C.c_size_t(0)
+        check(lib().pcs_job_checkpoint(self.h, None, 0, C.byref(n)), "pcs_job_checkpoint")
+        buf = C.create_string_buffer(n.value)
+        check(lib().pcs_job_checkpoint(self.h, buf, n.value, C.byref(n)), "pcs_job_checkpoint")
+        return buf.raw[:n.value]
+
+    def restore(self, data: bytes) -> None:
+        """Load a checkpoint into this job (created with the same parameters,
+        observed data and seed, not yet run)."""
+        buf = C.create_string_buffer(bytes(data), len(data))
+        check(lib().pcs_job_restore(self.h, buf, len(data)), "pcs_job_restore")
+
     def close(self):
         if self.h:
             check(lib().pcs_job_destroy(self.h), "pcs_job_destroy")

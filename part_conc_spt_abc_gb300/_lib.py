@@ -141,6 +141,8 @@ SIGNATURES = {
     "pcs_job_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "pcs_job_info_get": (C.c_int, [C.c_void_p, C.POINTER(JobInfo)]),
     "pcs_job_output": (C.c_int, [C.c_void_p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p]),
+    "pcs_job_checkpoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "pcs_job_restore": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "pcs_serve_submit": (C.c_int, [C.c_void_p, C.c_void_p]),
     "pcs_serve_step": (C.c_int, [C.c_void_p, _u32p]),
     "pcs_serve_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),

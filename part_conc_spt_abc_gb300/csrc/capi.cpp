@@ -366,6 +366,28 @@ pcs_status pcs_job_step(pcs_job* job, int* done)
     });
 }
 
+pcs_status pcs_job_checkpoint(pcs_job* job, void* buf, size_t cap, size_t* bytes)
+{
+    return guard([&] {
+        Job& j = J_(job);
+        need(bytes, "bytes");
+        const size_t n = j.checkpoint_bytes();
+        *bytes = n;
+        if (!buf) return;
+        if (cap < n) throw Error(PCS_ERR_INVALID_ARGUMENT, "checkpoint buffer too small");
+        j.save_state(buf);
+    });
+}
+
+pcs_status pcs_job_restore(pcs_job* job, const void* buf, size_t bytes)
+{
+    return guard([&] {
+        Job& j = J_(job);
+        need(buf, "buf");
+        j.load_state(buf, bytes);
+    });
+}
+
 pcs_status pcs_job_info_get(pcs_job* job, pcs_job_info* out)
 {
     return guard([&] {

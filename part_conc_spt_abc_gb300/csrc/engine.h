@@ -134,6 +134,10 @@ struct Job {
     uint64_t arena_bytes() const;
     void build_device_state(); /* allocate arena, observed histogram, prior population */
     void output(double* m, double* s, double* c, double* az, double* dist, double* w) const;
+    /* checkpoint.cpp: the job's state between rounds as a byte blob, and back */
+    size_t checkpoint_bytes() const;
+    void save_state(void* buf) const;
+    void load_state(const void* buf, size_t bytes);
 };
 
 /* shared-memory histogram words for a tile of tile_rows rows of `bins` bins */
