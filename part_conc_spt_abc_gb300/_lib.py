@@ -14,6 +14,7 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpcs.so")
 ACCEL_PATH = os.path.join(HERE, "bin", "accel")
+COMPARE_PATH = os.path.join(HERE, "bin", "compare")
 CSRC = os.path.join(HERE, "csrc")
 
 MAX_COMPONENTS = 8
