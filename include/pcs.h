@@ -375,6 +375,13 @@ pcs_status pcs_scan_distance_noalloc(uint32_t* d_hist, const uint32_t* d_ref_sat
 /* Observed cumulative histogram from K / DE lists, on the device. */
 pcs_status pcs_observed_sat(pcs_ctx* ctx, const uint32_t* K, const double* DE, size_t n,
                             uint32_t rows, uint32_t bins, double ub_de, uint32_t* sat_out);
+/* The same in the Julia path's conventions (src/cpu/estimate.jl:32-40):
+ * kmax x bins (row K-1 holds tracks of K frames, K = 1..kmax), DE binned by
+ * ceil(DE / (ub_de / bins)) into 1..bins (so DE = 0 and DE > ub_de are
+ * dropped), then the same 2-D inclusive prefix sums.  A K outside 1..kmax is
+ * an error (Julia raises a bounds error). */
+pcs_status pcs_observed_sat_julia(pcs_ctx* ctx, const uint32_t* K, const double* DE, size_t n,
+                                  uint32_t kmax, uint32_t bins, double ub_de, uint32_t* sat_out);
 
 /* Raw Philox words of one particle's stream block (checks the counter layout). */
 pcs_status pcs_debug_particle_stream(pcs_ctx* ctx, uint64_t seed, uint32_t slot, uint32_t trial,

@@ -88,6 +88,8 @@ def lib():
                                           C.c_uint32, C.c_uint32, _u32p, C.POINTER(OrcCounts)]
         L.orc_simulate_philox.restype = C.c_int
         L.orc_observed_sat.argtypes = [_u32p, _f64p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_double, _u32p]
+        L.orc_observed_sat_julia.argtypes = L.orc_observed_sat.argtypes
+        L.orc_observed_sat_julia.restype = C.c_int
         L.orc_observed_sat.restype = C.c_int
         L.orc_distance_kdist.argtypes = [_u32p, _u32p, C.c_uint32, C.c_uint32, _u32p, _u64p, _u64p]
         L.orc_distance_kdist.restype = C.c_float
@@ -274,6 +276,18 @@ def observed_sat(K, DE, R, B, ub_de):
     rc = lib().orc_observed_sat(ptr(K, C.c_uint32), ptr(DE, C.c_double), len(K), R, B, ub_de, ptr(sat, C.c_uint32))
     if rc != 0:
         raise ValueError("observed track outside the histogram")
+    return sat
+
+
+def observed_sat_julia(K, DE, kmax, B, ub_de):
+    """Observed cumulative histogram in the Julia path's conventions."""
+    K = np.ascontiguousarray(K, np.uint32)
+    DE = np.ascontiguousarray(DE, np.float64)
+    sat = np.zeros((kmax, B), np.uint32)
+    rc = lib().orc_observed_sat_julia(ptr(K, C.c_uint32), ptr(DE, C.c_double), len(K), kmax, B, ub_de,
+                                      ptr(sat, C.c_uint32))
+    if rc != 0:
+        raise ValueError("observed track length outside 1..kmax")
     return sat
 
 

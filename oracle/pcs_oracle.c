@@ -497,6 +497,28 @@ int orc_simulate_julia(uint32_t C, const double* m, const double* c, double ax, 
     return 0;
 }
 
+int orc_observed_sat_julia(const uint32_t* K, const double* DE, size_t n, uint32_t kmax, uint32_t B,
+                           double ub_de, uint32_t* sat)
+{
+    const double d_de = ub_de / (double)B; /* estimate.jl:29 */
+    memset(sat, 0, sizeof(uint32_t) * (size_t)kmax * B);
+    int rc = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const double q = ceil(DE[i] / d_de);
+        if (!(q >= 1.0 && q <= (double)B)) continue;
+        if (K[i] < 1u || K[i] > kmax) {
+            rc = -1;
+            continue;
+        }
+        sat[(size_t)(K[i] - 1u) * B + (size_t)q - 1u] += 1u;
+    }
+    for (uint32_t c = 0; c < B; ++c)
+        for (uint32_t r = 1; r < kmax; ++r) sat[(size_t)r * B + c] += sat[(size_t)(r - 1) * B + c];
+    for (uint32_t r = 0; r < kmax; ++r)
+        for (uint32_t c = 1; c < B; ++c) sat[(size_t)r * B + c] += sat[(size_t)r * B + c - 1];
+    return rc;
+}
+
 double orc_distance_julia(const int64_t* H, const int64_t* Hsim, uint32_t kmax, uint32_t B)
 {
     /* cumsum(cumsum(H - Hsim, 1), 2) then log10(sum(.^2)) */

@@ -146,6 +146,11 @@ int orc_simulate_julia(uint32_t C, const double* m, const double* c, double ax, 
                        double deltat, uint32_t kmin, uint32_t B, double ub_de,
                        const orc_replay_f64* rp, int64_t* H /* kmax x B, row-major */);
 double orc_distance_julia(const int64_t* H, const int64_t* Hsim, uint32_t kmax, uint32_t B);
+/* The Julia path's observed histogram (estimate.jl:32-40) and its 2-D
+ * inclusive prefix sums: kmax x B, row K-1, bin ceil(DE / (ub_de/B)) - 1
+ * for 1 <= ceil(..) <= B.  Returns -1 for a K outside 1..kmax. */
+int orc_observed_sat_julia(const uint32_t* K, const double* DE, size_t n, uint32_t kmax, uint32_t B,
+                           double ub_de, uint32_t* sat);
 
 /* PMC pieces, Float64 (simulation_impl.inl:24-79,733-887). */
 double orc_var_uncorrected(const double* x, size_t n, size_t stride);

@@ -393,12 +393,15 @@ def scan_distance(ctx: Context, hist: np.ndarray, ref_sat: np.ndarray, want_cum:
     return res
 
 
-def observed_sat(ctx: Context, K, DE, rows: int, bins: int, ub_de: float) -> np.ndarray:
+def observed_sat(ctx: Context, K, DE, rows: int, bins: int, ub_de: float, julia: bool = False) -> np.ndarray:
+    """Observed cumulative histogram on the device; julia=True uses the Julia
+    path's conventions (rows = kmax for K = 1..kmax, ceil binning)."""
     K = np.ascontiguousarray(K, np.uint32)
     DE = np.ascontiguousarray(DE, np.float64)
     out = np.zeros((rows, bins), np.uint32)
-    check(lib().pcs_observed_sat(ctx.h, _p(K, C.c_uint32), _p(DE, C.c_double), len(K), rows, bins, ub_de,
-                                 _p(out, C.c_uint32)), "pcs_observed_sat")
+    fn = lib().pcs_observed_sat_julia if julia else lib().pcs_observed_sat
+    check(fn(ctx.h, _p(K, C.c_uint32), _p(DE, C.c_double), len(K), rows, bins, ub_de, _p(out, C.c_uint32)),
+          "pcs_observed_sat")
     return out
 
 

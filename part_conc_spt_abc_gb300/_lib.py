@@ -165,6 +165,8 @@ SIGNATURES = {
     "pcs_scan_distance_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                             C.c_void_p, C.c_void_p]),
     "pcs_observed_sat": (C.c_int,[C.c_void_p, _u32p, _f64p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_double, _u32p]),
+    "pcs_observed_sat_julia": (C.c_int, [C.c_void_p, _u32p, _f64p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_double,
+                                         _u32p]),
     "pcs_debug_particle_stream": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                             C.c_uint32, C.c_uint32, _u32p]),
 }

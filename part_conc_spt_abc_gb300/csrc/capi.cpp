@@ -737,6 +737,31 @@ pcs_status pcs_observed_sat(pcs_ctx* ctx, const uint32_t* K, const double* DE, s
     });
 }
 
+pcs_status pcs_observed_sat_julia(pcs_ctx* ctx, const uint32_t* K, const double* DE, size_t n, uint32_t kmax,
+                                  uint32_t bins, double ub_de, uint32_t* sat_out)
+{
+    return guard([&] {
+        Ctx& c = C_(ctx);
+        need(sat_out, "sat_out");
+        if (n && (!K || !DE)) throw Error(PCS_ERR_INVALID_ARGUMENT, "K/DE are NULL");
+        if (kmax == 0 || bins == 0) throw Error(PCS_ERR_INVALID_ARGUMENT, "kmax and bins must be positive");
+        cudaStream_t st = c.stream;
+        DevTmp t;
+        const uint64_t RB = (uint64_t)kmax * bins;
+        uint32_t* dK = t.get<uint32_t>(n);
+        double* dDE = t.get<double>(n);
+        uint32_t* dS = t.get<uint32_t>(RB);
+        if (n) {
+            PCS_CUDA(cudaMemcpyAsync(dK, K, n * 4, cudaMemcpyHostToDevice, st));
+            PCS_CUDA(cudaMemcpyAsync(dDE, DE, n * 8, cudaMemcpyHostToDevice, st));
+        }
+        PCS_CUDA(launch_observed_sat_julia(dK, dDE, n, kmax, bins, ub_de, dS, c.err.as<uint32_t>(), st));
+        PCS_CUDA(cudaMemcpyAsync(sat_out, dS, RB * 4, cudaMemcpyDeviceToHost, st));
+        PCS_CUDA(cudaStreamSynchronize(st));
+        check_err_word(c);
+    });
+}
+
 pcs_status pcs_debug_particle_stream(pcs_ctx* ctx, uint64_t seed, uint32_t slot, uint32_t trial,
                                      uint32_t generation, uint32_t particle, uint32_t block, uint32_t out[4])
 {

@@ -656,6 +656,25 @@ __global__ void k_observed_bin(const uint32_t* K, const double* DE, size_t n, ui
     }
 }
 
+/* the Julia path's observed histogram (src/cpu/estimate.jl:32-40): kmax
+ * rows for K = 1..kmax, bin ceil(DE / width) kept when in 1..bins, i.e.
+ * (0, w] bins; a K outside 1..kmax sets the bounds bit (Julia throws). */
+__global__ void k_observed_bin_julia(const uint32_t* K, const double* DE, size_t n, uint32_t kmax,
+                                     uint32_t bins, double ub_de, uint32_t* sat, uint32_t* err)
+{
+    const double width = ub_de / (double)bins;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double q = ceil(DE[i] / width);
+        if (!(q >= 1.0 && q <= (double)bins)) continue;
+        const uint32_t k = K[i];
+        if (k < 1u || k > kmax) {
+            atomicOr(err, PCS_ERRBIT_HIST_BOUNDS);
+            continue;
+        }
+        atomicAdd(sat + (uint64_t)(k - 1u) * bins + (uint64_t)q - 1u, 1u);
+    }
+}
+
 /* column-wise then row-wise partial sums; also writes the transpose */
 __global__ void k_observed_cols(uint32_t rows, uint32_t bins, uint32_t* sat)
 {
@@ -724,6 +743,17 @@ cudaError_t launch_observed_sat(const uint32_t* K, const double* DE, size_t n, u
     if (n) k_observed_bin<<<(unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, st>>>(K, DE, n, rows, bins, ub_de, sat, err);
     k_observed_cols<<<(bins + 127) / 128, 128, 0, st>>>(rows, bins, sat);
     k_observed_rows<<<(rows + 127) / 128, 128, 0, st>>>(rows, bins, sat, sat_t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_observed_sat_julia(const uint32_t* K, const double* DE, size_t n, uint32_t kmax,
+                                      uint32_t bins, double ub_de, uint32_t* sat, uint32_t* err, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(sat, 0, sizeof(uint32_t) * (size_t)kmax * bins, st);
+    if (e != cudaSuccess) return e;
+    if (n) k_observed_bin_julia<<<(unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, st>>>(K, DE, n, kmax, bins, ub_de, sat, err);
+    k_observed_cols<<<(bins + 127) / 128, 128, 0, st>>>(kmax, bins, sat);
+    k_observed_rows<<<(kmax + 127) / 128, 128, 0, st>>>(kmax, bins, sat, nullptr);
     return cudaGetLastError();
 }
 

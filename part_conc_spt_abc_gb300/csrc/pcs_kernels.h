@@ -160,6 +160,8 @@ cudaError_t launch_finalize(const PmcArgs& a, uint32_t n_jobs, uint32_t max_n, c
 cudaError_t launch_observed_sat(const uint32_t* K, const double* DE, size_t n, uint32_t rows,
                                 uint32_t bins, double ub_de, uint32_t* sat, uint32_t* sat_t,
                                 uint32_t* err, cudaStream_t st);
+cudaError_t launch_observed_sat_julia(const uint32_t* K, const double* DE, size_t n, uint32_t kmax,
+                                      uint32_t bins, double ub_de, uint32_t* sat, uint32_t* err, cudaStream_t st);
 
 } // namespace pcs
 

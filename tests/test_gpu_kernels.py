@@ -80,6 +80,17 @@ def test_observed_sat_matches_oracle(pcs, ctx, oracle):
     np.testing.assert_array_equal(pcs.observed_sat(ctx, K, DE, R, B, ub), oracle.observed_sat(K, DE, R, B, ub))
 
 
+def test_observed_sat_julia_matches_oracle(pcs, ctx, oracle):
+    rng = np.random.default_rng(6)
+    kmax, B, ub = 300, 128, 20.0
+    K = rng.integers(1, kmax + 1, 40000)
+    DE = np.concatenate([rng.gamma(2.0, 2.0, 39970), np.zeros(10), np.arange(1, 21) * (ub / B)])
+    np.testing.assert_array_equal(pcs.observed_sat(ctx, K, DE, kmax, B, ub, julia=True),
+                                  oracle.observed_sat_julia(K, DE, kmax, B, ub))
+    with pytest.raises(pcs.PcsError):
+        pcs.observed_sat(ctx, np.array([kmax + 1]), np.array([1.0]), kmax, B, ub, julia=True)
+
+
 def test_philox_stream_layout(pcs, ctx, oracle):
     for seed, slot, trial, gen, n, blk in [(0, 0, 0, 0, 0, 0), (0xDEADBEEF12345678, 17, 3, 5, 999, 2),
                                            (42, 4095, 0xFFFFF, 4095, 123456, 77)]:

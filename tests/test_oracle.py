@@ -109,3 +109,22 @@ def test_pmc_pieces(oracle):
     np.testing.assert_allclose(out, ref / ref.sum(), rtol=1e-12)
     assert oracle.lib().orc_displace(0.5, 0.7, 0.0, 1.0) == pytest.approx(0.8)
     assert oracle.lib().orc_displace(0.5, -0.9, 0.0, 1.0) == pytest.approx(0.4)
+
+
+def test_observed_sat_julia_matches_numpy_restatement(oracle):
+    """estimate.jl:32-40 restated with numpy (ceil binning, K = 1..kmax rows)
+    against the C oracle, including DE = 0, DE on bin edges and DE > ub."""
+    rng = np.random.default_rng(12)
+    kmax, B, ub = 57, 40, 8.0
+    K = rng.integers(1, kmax + 1, 5000)
+    DE = np.concatenate([rng.uniform(0, 9.0, 4970), np.zeros(10), np.arange(1, 21) * (ub / B)])
+    want = np.zeros((kmax, B), np.int64)
+    for k, de in zip(K, DE):
+        idx = int(np.ceil(de / (ub / B)))
+        if 1 <= idx <= B:
+            want[k - 1, idx - 1] += 1
+    want = np.cumsum(np.cumsum(want, 0), 1)
+    got = oracle.observed_sat_julia(K, DE, kmax, B, ub)
+    assert np.array_equal(got, want)
+    with pytest.raises(ValueError):
+        oracle.observed_sat_julia(np.array([0]), np.array([1.0]), kmax, B, ub)
