@@ -87,6 +87,8 @@ def lib():
         L.orc_simulate_philox.argtypes = [C.POINTER(OrcSetup), C.POINTER(OrcRun), C.c_uint64, C.c_uint32,
                                           C.c_uint32, C.c_uint32, _u32p, C.POINTER(OrcCounts)]
         L.orc_simulate_philox.restype = C.c_int
+        L.orc_simulate_philox_split.argtypes = L.orc_simulate_philox.argtypes
+        L.orc_simulate_philox_split.restype = C.c_int
         L.orc_observed_sat.argtypes = [_u32p, _f64p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_double, _u32p]
         L.orc_observed_sat_julia.argtypes = L.orc_observed_sat.argtypes
         L.orc_observed_sat_julia.restype = C.c_int
@@ -238,12 +240,14 @@ def simulate_replay(st: Setup, u, z, sig=None):
     return hist, (cnt.closed, cnt.recorded)
 
 
-def simulate_philox(st: Setup, seed: int, slot: int = 0, trial: int = 0, generation: int = 0):
+def simulate_philox(st: Setup, seed: int, slot: int = 0, trial: int = 0, generation: int = 0, split: bool = False):
+    """Forward model on the product's Philox streams; split=True is the
+    slab-split walk, False the per-step walk."""
     s, r, keep = _structs(st)
     hist = np.zeros((st.R, st.B), np.uint32)
     cnt = OrcCounts()
-    rc = lib().orc_simulate_philox(C.byref(s), C.byref(r), seed, slot, trial, generation, ptr(hist, C.c_uint32),
-                                   C.byref(cnt))
+    fn = lib().orc_simulate_philox_split if split else lib().orc_simulate_philox
+    rc = fn(C.byref(s), C.byref(r), seed, slot, trial, generation, ptr(hist, C.c_uint32), C.byref(cnt))
     if rc != 0:
         raise RuntimeError(f"orc_simulate_philox failed: {rc}")
     return hist, (cnt.closed, cnt.recorded)

@@ -208,9 +208,114 @@ static void bm_pair(uint32_t ra, uint32_t rb, float* n0, float* n1)
     *n1 = (float)(rad * cos((double)t));
 }
 
-int orc_simulate_philox(const orc_setup* s, const orc_run* r, uint64_t seed, uint32_t slot,
-                        uint32_t trial, uint32_t generation, uint32_t* hist,
-                        orc_track_counts* counts)
+/* Track bookkeeping of one step (kernel-simulate.inl:70-93). */
+static void track_step(const orc_setup* s, uint32_t* hist, orc_track_counts* counts, int det, float de_step,
+                       uint32_t* k, float* de)
+{
+    if (det) {
+        ++*k;
+        if (*k >= 2u) *de = *de + de_step;
+    } else {
+        if (*k >= s->kmin) record(s, hist, *k, *de, counts);
+        *k = 0;
+        *de = 0.0f;
+    }
+}
+
+/* The slab-split walk of one particle (steps 1..frames-1): the same model as
+ * the per-step walk with fewer draws.  Steps go in groups of four (m <= 4 in
+ * the last group); per group:
+ *   z: four normals from one Philox block, z walked step by step exactly;
+ *   x, y: the group's summed displacement drawn at once, S = sd sqrt(m) n,
+ *     applied with one wrap;
+ *   if any z of the group lies in the detection slab, the group's x, y steps
+ *     are drawn conditionally on their sum (Gaussian bridge:
+ *     d_i = S/m + sd (n_i - mean n), exactly i.i.d. N(0, sd^2) again), walked
+ *     from the group's start and checked for detection; otherwise nothing in
+ *     the group is detected.
+ * Blocks per group pair h (groups 2h, 2h+1): 2+8h z(2h), 3+8h z(2h+1),
+ * 4+8h the sums of both groups, 5+8h..6+8h the x, y steps of group 2h,
+ * 7+8h..8+8h those of group 2h+1. */
+static void walk_split(const orc_setup* s, uint32_t* hist, orc_track_counts* counts, uint32_t ctr[4],
+                       const uint32_t key[2], uint32_t frames, float sd, float half_az, float* px, float* py,
+                       float* pz, uint32_t* pk, float* pde)
+{
+    static const float sqrt_m[5] = {0.0f, 1.0f, 1.41421356237f, 1.73205080757f, 2.0f};
+    static const float inv_m[5] = {0.0f, 1.0f, 0.5f, 0.333333333333f, 0.25f};
+    float x = *px, y = *py, z = *pz, de = *pde;
+    uint32_t k = *pk;
+    const uint32_t steps = frames > 0u ? frames - 1u : 0u;
+    const uint32_t groups = (steps + 3u) / 4u;
+    uint32_t w[4];
+    float agg[4] = {0, 0, 0, 0};
+    for (uint32_t g = 0; g < groups; ++g) {
+        const uint32_t m = (steps - 4u * g < 4u) ? steps - 4u * g : 4u;
+        const uint32_t base = 2u + 8u * (g >> 1), odd = g & 1u;
+        float nz[4];
+        ctr[1] = base + odd;
+        orc_philox4x32_10(ctr, key, w);
+        bm_pair(w[0], w[1], &nz[0], &nz[1]);
+        bm_pair(w[2], w[3], &nz[2], &nz[3]);
+        if (!odd) {
+            ctr[1] = base + 2u;
+            orc_philox4x32_10(ctr, key, w);
+            bm_pair(w[0], w[1], &agg[0], &agg[1]);
+            bm_pair(w[2], w[3], &agg[2], &agg[3]);
+        }
+        uint32_t zbits = 0;
+        for (uint32_t i = 0; i < m; ++i) {
+            const float dz = sd * nz[i];
+            z = periodic_bounds(z + dz, s->half_lz);
+            if (fabsf(z) <= half_az) zbits |= 1u << i;
+        }
+        const float sds = sd * sqrt_m[m];
+        const float sx = sds * agg[2 * odd], sy = sds * agg[2 * odd + 1];
+        const float xs = x, ys = y;
+        x = periodic_bounds(x + sx, s->half_lx);
+        y = periodic_bounds(y + sy, s->half_ly);
+        if (!zbits) {
+            track_step(s, hist, counts, 0, 0.0f, &k, &de);
+            continue;
+        }
+        float nx[4], ny[4];
+        ctr[1] = base + 3u + 2u * odd;
+        orc_philox4x32_10(ctr, key, w);
+        bm_pair(w[0], w[1], &nx[0], &ny[0]);
+        bm_pair(w[2], w[3], &nx[1], &ny[1]);
+        ctr[1] = base + 4u + 2u * odd;
+        orc_philox4x32_10(ctr, key, w);
+        bm_pair(w[0], w[1], &nx[2], &ny[2]);
+        bm_pair(w[2], w[3], &nx[3], &ny[3]);
+        float mx = 0.0f, my = 0.0f;
+        for (uint32_t i = 0; i < m; ++i) {
+            mx = mx + nx[i];
+            my = my + ny[i];
+        }
+        mx = mx * inv_m[m];
+        my = my * inv_m[m];
+        const float cx = sx * inv_m[m], cy = sy * inv_m[m];
+        float xx = xs, yy = ys;
+        for (uint32_t i = 0; i < m; ++i) {
+            const float dx = cx + sd * (nx[i] - mx);
+            const float dy = cy + sd * (ny[i] - my);
+            xx = periodic_bounds(xx + dx, s->half_lx);
+            yy = periodic_bounds(yy + dy, s->half_ly);
+            const int det = ((zbits >> i) & 1u) && fabsf(xx) <= s->half_ax && fabsf(yy) <= s->half_ay;
+            const float dx2 = dx * dx;
+            const float dy2 = dy * dy;
+            track_step(s, hist, counts, det, dx2 + dy2, &k, &de);
+        }
+    }
+    *px = x;
+    *py = y;
+    *pz = z;
+    *pk = k;
+    *pde = de;
+}
+
+static int simulate_philox_(const orc_setup* s, const orc_run* r, uint64_t seed, uint32_t slot,
+                            uint32_t trial, uint32_t generation, uint32_t* hist,
+                            orc_track_counts* counts, int split)
 {
     orc_track_counts local = {0, 0};
     if (!counts) counts = &local;
@@ -249,6 +354,11 @@ int orc_simulate_philox(const orc_setup* s, const orc_run* r, uint64_t seed, uin
             }
             float de = 0.0f;
             uint32_t k = detected(x, y, z, half_az, s) ? 1u : 0u;
+            if (split) {
+                walk_split(s, hist, counts, ctr, key, frames, sd, half_az, &x, &y, &z, &k, &de);
+                if (k >= s->kmin) record(s, hist, k, de, counts);
+                continue;
+            }
             float nn[12];
             for (uint32_t frame = 1; frame < frames; ++frame) {
                 const uint32_t g = (frame - 1) >> 2, sub = (frame - 1) & 3u;
@@ -284,6 +394,20 @@ int orc_simulate_philox(const orc_setup* s, const orc_run* r, uint64_t seed, uin
         }
     }
     return 0;
+}
+
+int orc_simulate_philox(const orc_setup* s, const orc_run* r, uint64_t seed, uint32_t slot,
+                        uint32_t trial, uint32_t generation, uint32_t* hist,
+                        orc_track_counts* counts)
+{
+    return simulate_philox_(s, r, seed, slot, trial, generation, hist, counts, 0);
+}
+
+int orc_simulate_philox_split(const orc_setup* s, const orc_run* r, uint64_t seed, uint32_t slot,
+                              uint32_t trial, uint32_t generation, uint32_t* hist,
+                              orc_track_counts* counts)
+{
+    return simulate_philox_(s, r, seed, slot, trial, generation, hist, counts, 1);
 }
 
 /* ------------------------------------------------------------------ */

@@ -115,6 +115,15 @@ int orc_simulate_philox(const orc_setup* s, const orc_run* r, uint64_t seed, uin
                         uint32_t trial, uint32_t generation, uint32_t* hist,
                         orc_track_counts* counts);
 
+/* The same model with the slab-split walk (walk_split in pcs_oracle.c): z
+ * walked per step, x and y drawn per group of four steps as their sum and,
+ * only where a z of the group lies in the detection slab, as the individual
+ * steps conditioned on that sum.  Same distribution of histograms as
+ * orc_simulate_philox from different draws. */
+int orc_simulate_philox_split(const orc_setup* s, const orc_run* r, uint64_t seed, uint32_t slot,
+                              uint32_t trial, uint32_t generation, uint32_t* hist,
+                              orc_track_counts* counts);
+
 /* Observed-data cumulative histogram (simulation_impl.inl:605-629). */
 int orc_observed_sat(const uint32_t* K, const double* DE, size_t n, uint32_t rows,
                      uint32_t bins, double ub_de, uint32_t* sat);

@@ -128,3 +128,39 @@ def test_observed_sat_julia_matches_numpy_restatement(oracle):
     assert np.array_equal(got, want)
     with pytest.raises(ValueError):
         oracle.observed_sat_julia(np.array([0]), np.array([1.0]), kmax, B, ub)
+
+
+def _ln_setup(oracle, mu, sd, parts, V=20, F=200, B=100):
+    import math
+    dt, kB, T, eta = 1 / 30, 1.380649e-23, 298.0, 0.95e-3
+    g = math.sqrt(2 * dt * kB * T * 1e21 / (3 * math.pi * eta))
+    sl2 = math.log1p(sd * sd / (mu * mu))
+    mul = math.log(mu) - 0.5 * sl2
+    st = oracle.Setup(2, 1, np.full(V, F, np.uint32), np.full(V, parts, np.uint32), 2,
+                      float(np.float32(4) * np.float32(dt)), (100.0, 80.0, 10.0), (50.0, 40.0),
+                      np.array([1.0], np.float32), np.array([2.0], np.float32), np.zeros(1, np.float32),
+                      float(np.float32(20.0 / B)), F + 1, B)
+    st.ln_scale = np.array([np.float32(g * math.exp(-0.5 * mul))] + [0] * 7, np.float32)
+    st.ln_shape = np.array([np.float32(-0.5 * math.sqrt(sl2))] + [0] * 7, np.float32)
+    return st
+
+
+@pytest.mark.parametrize("mu,F", [(175.0, 200), (60.0, 100)])
+def test_split_walk_has_the_per_step_distribution(oracle, mu, F):
+    """The slab-split walk (x, y drawn per group as a sum and, near the
+    detection slab, as a Gaussian bridge) against the per-step walk on
+    independent streams: histogram total, mean track length and mean DE bin
+    within 4 Monte-Carlo standard errors over 48 replicas each."""
+    st = _ln_setup(oracle, mu, 10.0, 128, F=F)
+
+    def moments(h):
+        R, B = h.shape
+        n = h.sum()
+        return np.array([n, (h * np.arange(R)[:, None]).sum() / n, (h * np.arange(B)[None, :]).sum() / n])
+
+    reps = 48
+    a = np.array([moments(oracle.simulate_philox(st, 3, slot=s)[0]) for s in range(reps)])
+    b = np.array([moments(oracle.simulate_philox(st, 4, slot=s, split=True)[0]) for s in range(reps)])
+    se = np.sqrt(a.var(0, ddof=1) / reps + b.var(0, ddof=1) / reps)
+    z = np.abs(a.mean(0) - b.mean(0)) / se
+    assert (z < 4.0).all(), (a.mean(0), b.mean(0), z)
