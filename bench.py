@@ -31,9 +31,19 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# algorithmic thread-operations per particle-step of the forward model
-# (Philox 0.75 calls x 80, Box-Muller 1.5 pairs x 14, walk/detect/DE 32)
+# Algorithmic thread-operations of the forward model, from the algorithm
+# (Philox4x32-10 call 80, Box-Muller pair 14):
+#   per-step walk, per particle-step: Philox 0.75 calls (60) + Box-Muller 1.5
+#     pairs (21) + walk, wrap, detection, DE (32) = 113;
+#   slab-split walk, per particle-step of the z pass: per group of four steps
+#     Philox 1.5 calls (120) + Box-Muller 3 pairs (42) + four z steps (20) +
+#     summed x, y (10) = 192, i.e. 48 per step;
+#   slab-split walk, per task (a group walked in x, y): Philox 2 calls (160) +
+#     Box-Muller 4 pairs (56) + bridge means (12) + four x, y steps with
+#     detection and DE (72) + track bookkeeping (12) = 312.
 OPS_PER_STEP = 113
+OPS_SPLIT_STEP = 48
+OPS_SPLIT_TASK = 312
 # bytes the distance kernel moves per histogram cell: read count, write zero,
 # read the observed cumulative histogram
 DIST_BYTES_PER_CELL = 12
@@ -343,6 +353,8 @@ def main():
     ap.add_argument("--plain", type=int, default=0, choices=[0, 1, 2],
                     help="time the plain form instead (1: reference launch geometry, 2: persistent grid) "
                          "over --steps generations")
+    ap.add_argument("--walk", default="step", choices=["step", "split"],
+                    help="forward-model walk on Philox streams: per step (default) or slab-split")
     ap.add_argument("--no-round-fill", action="store_true",
                     help="no extra trials for rounds that would underfill the GPU")
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3],
@@ -375,6 +387,7 @@ def main():
     inp, truth = {0: W.config0, 1: W.config1, 2: W.config2, 3: W.config3}[cfg](ctx, seed=0, generations=gens)
     if not args.no_autotune and cfg != 3:
         ctx.autotune(inp)
+    ctx.set_tuning(walk=1 if args.walk == "split" else 2)
     if args.no_round_fill:
         ctx.set_tuning(round_fill=0xFFFFFFFF)
     if cfg == 2:
@@ -382,7 +395,7 @@ def main():
     if cfg == 3:
         ctx.set_tuning(round_capacity=64)
     t = ctx.tuning
-    tune = dict(round_fill=t.round_fill, block=t.block_size, ppt=t.particles_per_thread, tile_rows=t.hist_tile_rows,
+    tune = dict(walk={1: "slab-split", 2: "per-step"}.get(t.walk, t.walk), round_fill=t.round_fill, block=t.block_size, ppt=t.particles_per_thread, tile_rows=t.hist_tile_rows,
                 warp_aggregate=t.warp_aggregate, chunk=t.chunk_particles, capacity=t.round_capacity,
                 autotuned=not args.no_autotune and cfg != 3)
 
@@ -444,7 +457,11 @@ def main():
     # ---- roofline of the dominant kernel (forward model: issue bound) -----
     sim_ms = ks.simulate_ms / max(1, ks.simulate_launches)
     steps_per_launch = ks.particle_steps / max(1, ks.simulate_launches)
-    achieved = steps_per_launch * OPS_PER_STEP / (sim_ms / 1e3) / 1e12
+    split = t.walk == 1
+    tasks_per_launch = ks.split_tasks / max(1, ks.simulate_launches)
+    ops_per_launch = (steps_per_launch * OPS_SPLIT_STEP + tasks_per_launch * OPS_SPLIT_TASK if split
+                      else steps_per_launch * OPS_PER_STEP)
+    achieved = ops_per_launch / (sim_ms / 1e3) / 1e12
     sm_count = device_sm_count(P, local)
     peak = sm_count * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
     traffic = simulate_traffic(sim_ms) if cfg == 1 else None
@@ -468,7 +485,11 @@ def main():
         "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tops/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": "k_simulate (fused forward model + histogram)",
-                     "achieved_def": f"{OPS_PER_STEP} algorithmic thread-ops per particle-step x steps per launch / launch time",
+                     "achieved_def": (f"({OPS_SPLIT_STEP} x particle-steps + {OPS_SPLIT_TASK} x x,y tasks) algorithmic "
+                                      "thread-ops per launch / launch time" if split else
+                                      f"{OPS_PER_STEP} algorithmic thread-ops per particle-step x steps per launch / "
+                                      "launch time"),
+                     "ops_per_particle_step": ops_per_launch / max(1.0, steps_per_launch),
                      "peak_def": f"{sm_count} SMs x 128 lanes x {peaks.get('sm_max_mhz', 2070.0)} MHz ({peak_src} clock)"},
         "roofline_distance": {"bound": "hbm", "achieved": dist_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                               "frac": dist_gbs / float(peaks.get("hbm_gbs", 6800.0)),

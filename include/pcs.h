@@ -153,6 +153,12 @@ typedef struct pcs_tuning {
                                    * proportionally more trials, up to the capacity.  Default:
                                    * one wave of the simulate launch (SMs x 2048 threads);
                                    * PCS_TUNE_ZERO: none */
+    uint32_t walk;                /* forward-model walk on Philox streams: 2 per step (default),
+                                   * 1 slab-split (z per step, x, y per group of four steps as
+                                   * their sum and, near the detection slab, as the steps
+                                   * conditioned on it).  Both draw histograms from the same
+                                   * distribution, from different draws; the autotuner never
+                                   * changes it.  Replayed draws always take the per-step walk. */
 } pcs_tuning;
 pcs_status pcs_get_tuning(pcs_ctx* ctx, pcs_tuning* out);
 pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t);
@@ -178,6 +184,7 @@ typedef struct pcs_kernel_stats {
     uint64_t proposals;           /* forward simulations */
     uint64_t particle_steps;      /* walk steps incl. initial placements */
     uint64_t histogram_cells;     /* R x B cells scanned by the distance kernel */
+    uint64_t split_tasks;         /* slab-split walk: groups of four steps walked in x, y */
 } pcs_kernel_stats;
 pcs_status pcs_get_kernel_stats(pcs_ctx* ctx, pcs_kernel_stats* out);
 pcs_status pcs_reset_kernel_stats(pcs_ctx* ctx);

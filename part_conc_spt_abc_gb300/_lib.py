@@ -61,7 +61,7 @@ class Tuning(C.Structure):
         ("block_size", C.c_uint32), ("particles_per_thread", C.c_uint32), ("hist_tile_rows", C.c_uint32),
         ("warp_aggregate", C.c_uint32), ("chunk_particles", C.c_uint32), ("round_capacity", C.c_uint32),
         ("max_speculation", C.c_uint32), ("use_graphs", C.c_uint32), ("plain_launch", C.c_uint32),
-        ("round_fill", C.c_uint32),
+        ("round_fill", C.c_uint32), ("walk", C.c_uint32),
     ]
 
 
@@ -79,7 +79,7 @@ class KernelStats(C.Structure):
         ("rounds", C.c_uint64), ("kernel_launches", C.c_uint64), ("simulate_launches", C.c_uint64),
         ("simulate_ms", C.c_double), ("distance_launches", C.c_uint64), ("distance_ms", C.c_double),
         ("round_ms", C.c_double), ("proposals", C.c_uint64), ("particle_steps", C.c_uint64),
-        ("histogram_cells", C.c_uint64),
+        ("histogram_cells", C.c_uint64), ("split_tasks", C.c_uint64),
     ]
 
 

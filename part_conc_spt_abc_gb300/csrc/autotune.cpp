@@ -46,7 +46,8 @@ static float time_config(Ctx& c, const Candidate& k, int reps)
     l.ppt = (int)k.ppt;
     l.aggregate = k.agg != 0;
     l.replay = false;
-    l.grid = c.sim_grid(l.block, k.ppt, l.aggregate, s.tile_words);
+    l.split = c.split_walk();
+    l.grid = c.sim_grid(l.block, k.ppt, l.aggregate, s.tile_words, l.split);
     float best = 1e30f;
     for (int r = 0; r < reps; ++r) {
         PCS_CUDA(cudaMemsetAsync(&rd->queue_head, 0, 4, c.stream));
@@ -101,7 +102,8 @@ void autotune(Ctx& c, const pcs_params& p, const pcs_observed& obs, pcs_tuning* 
                         if (t == 0 && g == 1) continue;
                         if ((size_t)t * B * 4u > 200u * 1024u) continue;
                         if (t > job.R) continue;
-                        SimLaunch l{0, b, (int)pp, false, g != 0};
+                        if (c.split_walk() && (pp != 1u || b != 256u)) continue; /* fixed shape */
+                        SimLaunch l{0, b, (int)pp, false, g != 0, c.split_walk()};
                         if (simulate_occupancy(l, t * B) < 1) continue;
                         grid.push_back({b, pp, t, g});
                     }

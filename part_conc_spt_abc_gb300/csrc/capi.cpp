@@ -206,6 +206,7 @@ pcs_status pcs_get_tuning(pcs_ctx* ctx, pcs_tuning* out)
         out->use_graphs = c.tune.use_graphs;
         out->plain_launch = c.tune.plain_launch;
         out->round_fill = c.tune.round_fill;
+        out->walk = c.tune.walk;
     });
 }
 
@@ -238,6 +239,10 @@ pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t)
             c.tune.plain_launch = t->plain_launch;
         }
         if (t->round_fill) c.tune.round_fill = t->round_fill == 0xFFFFFFFFu ? 0u : t->round_fill;
+        if (t->walk) {
+            if (t->walk != 1u && t->walk != 2u) throw Error(PCS_ERR_INVALID_ARGUMENT, "walk must be 1 (slab-split) or 2 (per step)");
+            c.tune.walk = t->walk;
+        }
         c.graph_dirty = true;
     });
 }
@@ -269,6 +274,7 @@ pcs_status pcs_get_kernel_stats(pcs_ctx* ctx, pcs_kernel_stats* out)
         Ctx& c = C_(ctx);
         need(out, "out");
         *out = c.stats;
+        out->split_tasks = c.read_sim_tasks() - c.sim_tasks_base;
     });
 }
 
@@ -277,6 +283,7 @@ pcs_status pcs_reset_kernel_stats(pcs_ctx* ctx)
     return guard([&] {
         Ctx& c = C_(ctx);
         std::memset(&c.stats, 0, sizeof c.stats);
+        c.sim_tasks_base = c.read_sim_tasks();
     });
 }
 
@@ -637,6 +644,7 @@ pcs_status pcs_simulate_hist(pcs_ctx* ctx, const pcs_setup* setup, const pcs_run
         l.ppt = replay ? 1 : (int)c.tune.ppt;
         l.replay = replay != nullptr;
         l.aggregate = c.tune.aggregate == 1u;
+        l.split = !replay && c.split_walk();
         int occ = simulate_occupancy(l, a.tile_words);
         l.grid = (uint32_t)std::max(1, occ) * (uint32_t)c.sm_count;
         PCS_CUDA(launch_simulate(a, l, st));

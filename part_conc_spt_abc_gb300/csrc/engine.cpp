@@ -404,6 +404,8 @@ Ctx::Ctx(int dev, int infl) : device(dev), inflight(infl > 0 ? infl : 1)
     tune.round_fill = (uint32_t)sm_count * 2048u; /* one full-occupancy wave of walkers */
     PCS_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     err.alloc(16);
+    sim_tasks.alloc(8);
+    PCS_CUDA(cudaMemset(sim_tasks.p, 0, 8));
     PCS_CUDA(cudaMemset(err.p, 0, 16));
     PCS_CUDA(cudaMallocHost((void**)&h_err, 16));
     PCS_CUDA(cudaMallocHost((void**)&h_status, sizeof(JobPmcDev) * kMaxRoundJobs));
@@ -443,9 +445,17 @@ uint32_t tile_words_for(uint32_t tile_rows, uint32_t bins)
     return (uint32_t)(rows * b);
 }
 
-uint32_t Ctx::sim_grid(uint32_t block, uint32_t ppt, bool agg, uint32_t tw) const
+uint64_t Ctx::read_sim_tasks()
 {
-    SimLaunch l{0, block, (int)ppt, false, agg};
+    unsigned long long v = 0;
+    PCS_CUDA(cudaStreamSynchronize(stream));
+    PCS_CUDA(cudaMemcpy(&v, sim_tasks.p, 8, cudaMemcpyDeviceToHost));
+    return (uint64_t)v;
+}
+
+uint32_t Ctx::sim_grid(uint32_t block, uint32_t ppt, bool agg, uint32_t tw, bool split) const
+{
+    SimLaunch l{0, block, (int)ppt, false, agg, split};
     int occ = simulate_occupancy(l, tw);
     if (occ < 1) occ = 1;
     return (uint32_t)(occ * sm_count);
@@ -554,12 +564,14 @@ void Ctx::enqueue_round()
     s.chunk = tune.chunk;
     s.tile_words = tile_words_for(tune.tile_rows, rb_max_b_);
     s.err = a.err;
+    s.tasks = sim_tasks.as<unsigned long long>();
     SimLaunch l{};
     l.block = tune.block;
     l.ppt = (int)tune.ppt;
     l.replay = false;
     l.aggregate = tune.aggregate == 1u;
-    l.grid = sim_grid(l.block, tune.ppt, l.aggregate, s.tile_words);
+    l.split = split_walk();
+    l.grid = sim_grid(l.block, tune.ppt, l.aggregate, s.tile_words, l.split);
     PCS_CUDA(cudaEventRecordWithFlags(ev_sim0, stream, cudaEventRecordExternal));
     PCS_CUDA(launch_simulate(s, l, stream));
     PCS_CUDA(cudaEventRecordWithFlags(ev_sim1, stream, cudaEventRecordExternal));

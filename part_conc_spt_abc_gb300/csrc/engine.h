@@ -60,6 +60,7 @@ struct Tuning {
     uint32_t use_graphs = 1;
     uint32_t plain_launch = 1; /* 1 reference geometry, 2 persistent grid */
     uint32_t round_fill = 0; /* particles a round is topped up to (0: none); set to one wave at open */
+    uint32_t walk = 2; /* forward-model walk on Philox streams: 1 slab-split, 2 per step */
 };
 
 struct Job;
@@ -78,6 +79,8 @@ struct Ctx {
     cudaStream_t stream = nullptr;
     Tuning tune;
     DevBuf err;              /* device error word */
+    DevBuf sim_tasks;        /* slab-split task counter (u64, cumulative) */
+    uint64_t sim_tasks_base = 0;
     uint32_t* h_err = nullptr;
     RoundBufs rb;
     JobPmcDev* h_status = nullptr; /* pinned mirror of the pmc table */
@@ -107,7 +110,9 @@ struct Ctx {
     void run_round(double* ms_out);
     void admit(Job* j);
     void retire(Job* j);
-    uint32_t sim_grid(uint32_t block, uint32_t ppt, bool agg, uint32_t tile_words) const;
+    uint32_t sim_grid(uint32_t block, uint32_t ppt, bool agg, uint32_t tile_words, bool split = false) const;
+    bool split_walk() const { return tune.walk == 1u; }
+    uint64_t read_sim_tasks();
 };
 
 struct Job {

@@ -26,6 +26,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pcs_common.h"
 #include "pcs_kernels.h"
 
@@ -154,6 +156,92 @@ __device__ __forceinline__ uint32_t video_of_(const uint32_t* prefix, uint32_t V
     return lo;
 }
 
+/* Item context of proposal s_prop (of job s_job). */
+__device__ __forceinline__ ItemCtx item_ctx_(const SimArgs& a, const JobDev& s_job, const PropDev& s_prop)
+{
+    ItemCtx c;
+    c.hlx = s_job.half_lx;
+    c.hly = s_job.half_ly;
+    c.hlz = s_job.half_lz;
+    c.two_hlx = 2.0f * s_job.half_lx;
+    c.two_hly = 2.0f * s_job.half_ly;
+    c.two_hlz = 2.0f * s_job.half_lz;
+    c.hax = s_job.half_ax;
+    c.hay = s_job.half_ay;
+    c.four_dt = s_job.four_delta_t;
+    c.dde = s_job.dde;
+    c.kmin = s_job.kmin;
+    c.B = s_job.B;
+    c.RB = s_job.R * s_job.B;
+    c.tile_rows = min(s_job.R, a.tile_words / max(s_job.B, 1u));
+    c.tile_words_used = c.tile_rows * s_job.B;
+    c.hist = a.hist + s_prop.hist_off;
+    c.err = a.err;
+    return c;
+}
+
+/* Loads work item `item`'s proposal and job blocks into shared memory. */
+__device__ __forceinline__ void load_item_(const SimArgs& a, uint32_t item, PropDev& s_prop, JobDev& s_job)
+{
+    const uint32_t tid = threadIdx.x;
+    const uint32_t p = a.item_prop[item];
+    if (tid < sizeof(PropDev) / 4) reinterpret_cast<uint32_t*>(&s_prop)[tid] = reinterpret_cast<const uint32_t*>(a.props + p)[tid];
+    __syncthreads();
+    if (tid < sizeof(JobDev) / 4) reinterpret_cast<uint32_t*>(&s_job)[tid] = reinterpret_cast<const uint32_t*>(a.jobs + s_prop.job)[tid];
+    __syncthreads();
+}
+
+/* Initial state of particle n (make_particle, utility.inl:60-99, and the
+ * particle's step sd): position, component, half depth, step sd, K. */
+template <bool REPLAY>
+__device__ __forceinline__ void init_walker_(const SimArgs& a, const ItemCtx& c, const JobDev& s_job,
+                                             const PropDev& s_prop, const uint32_t* prefix, uint32_t n,
+                                             uint32_t slot, uint32_t gt, uint32_t k0, uint32_t k1, Walker& q)
+{
+    const uint32_t V = s_job.V, C = s_job.C, model = s_job.model;
+    const uint32_t v = video_of_(prefix, V, n);
+    q.F = __ldg(s_job.frames + v);
+    float u0, u1, u2, u3;
+    if (REPLAY) {
+        const float* u = a.rp_uniforms + 4ull * n;
+        u0 = u[0];
+        u1 = u[1];
+        u2 = u[2];
+        u3 = u[3];
+    } else {
+        q.ph = pcs_philox_prepare(n, slot, gt, k0, k1);
+        pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 0u));
+        u0 = pcs_u01_24(r.x);
+        u1 = pcs_u01_24(r.y);
+        u2 = pcs_u01_24(r.z);
+        u3 = pcs_u01_24(r.w);
+    }
+    /* make_particle (utility.inl:60-99): halfL * (2u - 1) */
+    q.x = __fmul_rn(c.hlx, __fsub_rn(2.0f * u0, 1.0f));
+    q.y = __fmul_rn(c.hly, __fsub_rn(2.0f * u1, 1.0f));
+    q.z = __fmul_rn(c.hlz, __fsub_rn(2.0f * u2, 1.0f));
+    uint32_t comp = (C > 1u) ? wrand_index_(u3, C, s_prop.pre_comp_prob) : 0u;
+    if (comp >= C) {
+        atomicOr(a.err, PCS_ERRBIT_COMPONENT);
+        comp = C - 1u;
+    }
+    q.haz = (model == PCS_DEV_MODEL_VARIABLE_Z) ? s_prop.half_az[comp] : s_prop.half_az[0];
+    if (model == PCS_DEV_MODEL_LOGNORMAL) {
+        if (REPLAY) {
+            q.sd = a.rp_sigmas[n];
+        } else {
+            pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 1u));
+            float z0, z1;
+            box_muller_(r.x, r.y, z0, z1);
+            q.sd = s_prop.sd_scale[comp] * expf(s_prop.sd_shape[comp] * z0);
+        }
+    } else {
+        q.sd = s_prop.sd_scale[comp];
+    }
+    const bool det = fabsf(q.z) <= q.haz && fabsf(q.x) <= c.hax && fabsf(q.y) <= c.hay;
+    q.k = det ? 1u : 0u;
+}
+
 } // namespace
 
 template <int PPT, bool REPLAY, bool AGG>
@@ -174,34 +262,10 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
         __syncthreads();
         const uint32_t item = s_item;
         if (item >= n_items) break;
-        const uint32_t p = a.item_prop[item];
-        if (tid < sizeof(PropDev) / 4) reinterpret_cast<uint32_t*>(&s_prop)[tid] = reinterpret_cast<const uint32_t*>(a.props + p)[tid];
-        __syncthreads();
-        if (tid < sizeof(JobDev) / 4) reinterpret_cast<uint32_t*>(&s_job)[tid] = reinterpret_cast<const uint32_t*>(a.jobs + s_prop.job)[tid];
-        __syncthreads();
-
-        ItemCtx c;
-        c.hlx = s_job.half_lx;
-        c.hly = s_job.half_ly;
-        c.hlz = s_job.half_lz;
-        c.two_hlx = 2.0f * s_job.half_lx;
-        c.two_hly = 2.0f * s_job.half_ly;
-        c.two_hlz = 2.0f * s_job.half_lz;
-        c.hax = s_job.half_ax;
-        c.hay = s_job.half_ay;
-        c.four_dt = s_job.four_delta_t;
-        c.dde = s_job.dde;
-        c.kmin = s_job.kmin;
-        c.B = s_job.B;
-        c.RB = s_job.R * s_job.B;
-        c.tile_rows = min(s_job.R, a.tile_words / max(s_job.B, 1u));
-        c.tile_words_used = c.tile_rows * s_job.B;
-        c.hist = a.hist + s_prop.hist_off;
-        c.err = a.err;
+        load_item_(a, item, s_prop, s_job);
+        const ItemCtx c = item_ctx_(a, s_job, s_prop);
 
         const uint32_t V = s_job.V;
-        const uint32_t C = s_job.C;
-        const uint32_t model = s_job.model;
         const uint32_t* prefix = a.counts + s_prop.counts_off + V; /* [V+1] */
         const uint32_t k0 = s_job.seed_lo, k1 = s_job.seed_hi;
         const uint32_t slot = s_prop.slot;
@@ -226,47 +290,7 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
                 q.sd = 0.0f;
                 q.haz = 0.0f;
                 if (n < a1) {
-                    const uint32_t v = video_of_(prefix, V, n);
-                    q.F = __ldg(s_job.frames + v);
-                    float u0, u1, u2, u3;
-                    if (REPLAY) {
-                        const float* u = a.rp_uniforms + 4ull * n;
-                        u0 = u[0];
-                        u1 = u[1];
-                        u2 = u[2];
-                        u3 = u[3];
-                    } else {
-                        q.ph = pcs_philox_prepare(n, slot, gt, k0, k1);
-                        pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 0u));
-                        u0 = pcs_u01_24(r.x);
-                        u1 = pcs_u01_24(r.y);
-                        u2 = pcs_u01_24(r.z);
-                        u3 = pcs_u01_24(r.w);
-                    }
-                    /* make_particle (utility.inl:60-99): halfL * (2u - 1) */
-                    q.x = __fmul_rn(c.hlx, __fsub_rn(2.0f * u0, 1.0f));
-                    q.y = __fmul_rn(c.hly, __fsub_rn(2.0f * u1, 1.0f));
-                    q.z = __fmul_rn(c.hlz, __fsub_rn(2.0f * u2, 1.0f));
-                    uint32_t comp = (C > 1u) ? wrand_index_(u3, C, s_prop.pre_comp_prob) : 0u;
-                    if (comp >= C) {
-                        atomicOr(a.err, PCS_ERRBIT_COMPONENT);
-                        comp = C - 1u;
-                    }
-                    q.haz = (model == PCS_DEV_MODEL_VARIABLE_Z) ? s_prop.half_az[comp] : s_prop.half_az[0];
-                    if (model == PCS_DEV_MODEL_LOGNORMAL) {
-                        if (REPLAY) {
-                            q.sd = a.rp_sigmas[n];
-                        } else {
-                            pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 1u));
-                            float z0, z1;
-                            box_muller_(r.x, r.y, z0, z1);
-                            q.sd = s_prop.sd_scale[comp] * expf(s_prop.sd_shape[comp] * z0);
-                        }
-                    } else {
-                        q.sd = s_prop.sd_scale[comp];
-                    }
-                    bool det = fabsf(q.z) <= q.haz && fabsf(q.x) <= c.hax && fabsf(q.y) <= c.hay;
-                    q.k = det ? 1u : 0u;
+                    init_walker_<REPLAY>(a, c, s_job, s_prop, prefix, n, slot, gt, k0, k1, q);
                     fmax = max(fmax, q.F);
                 }
             }
@@ -317,6 +341,277 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
 }
 
 /* ----------------------------------------------------------------------- */
+/* The slab-split walk (k_simulate_split).
+ *
+ * Same model as k_simulate, fewer draws: a particle can only be detected
+ * while its z lies in the detection slab (|z| <= half depth), and the x, y
+ * steps taken while z is outside it matter only through their sum.  Steps
+ * go in groups of four (m <= 4 in the last group).  The CTA (256 threads,
+ * one particle each) works in chunks of kSplitG groups, in three phases
+ * separated by barriers:
+ *   Z  every thread walks z step by step exactly (four normals per group)
+ *      and moves x, y by the group's summed displacement S = sd sqrt(m) n;
+ *      a group with any z in the slab becomes a task in the CTA's queue;
+ *   T  the CTA's threads take the queued tasks densely: a task draws its
+ *      group's x, y steps conditioned on their sum (Gaussian bridge,
+ *      d_i = S/m + sd (n_i - mean n), exactly i.i.d. N(0, sd^2) again),
+ *      walks them from the group's start and stores each step's detection
+ *      bit and dx^2 + dy^2;
+ *   S  each thread runs the reference's track bookkeeping
+ *      (kernel-simulate.inl:70-93) over its groups in time order; a group
+ *      without a task is undetected from its first step.
+ * The joint law of the positions at every frame is the per-step walk's, so
+ * the histograms have the same distribution (from different draws); the
+ * CPU oracle's orc_simulate_philox_split follows the same blocks and
+ * arithmetic.  Philox blocks of particle n per group pair h (groups 2h,
+ * 2h+1): 2+8h z(2h), 3+8h z(2h+1), 4+8h both groups' sums, 5+8h..6+8h the
+ * x, y steps of group 2h, 7+8h..8+8h those of group 2h+1. */
+
+constexpr uint32_t kSplitThreads = 256;
+constexpr uint32_t kSplitG = 6; /* groups per chunk: even, so group pairs stay in one chunk */
+constexpr uint32_t kSplitCap = kSplitThreads * kSplitG;
+
+struct SplitShared {
+    float xs[kSplitCap], ys[kSplitCap], sx[kSplitCap], sy[kSplitCap]; /* in; out: dx^2 + dy^2 per step */
+    float sd[kSplitCap];
+    uint32_t meta[kSplitCap]; /* owner << 16 | group-in-chunk << 8 | m << 4 | in-slab bits (detection bits out) */
+    uint16_t idx[kSplitG][kSplitThreads]; /* task of (group-in-chunk, thread) */
+    uint32_t count;
+};
+
+namespace {
+
+__device__ __forceinline__ float split_sqrt_m_(uint32_t m)
+{
+    return m == 4u ? 2.0f : (m == 3u ? 1.73205080757f : (m == 2u ? 1.41421356237f : 1.0f));
+}
+
+__device__ __forceinline__ float split_inv_m_(uint32_t m)
+{
+    return m == 4u ? 0.25f : (m == 3u ? 0.333333333333f : (m == 2u ? 0.5f : 1.0f));
+}
+
+template <bool AGG>
+__device__ __forceinline__ void close_track_(const ItemCtx& c, uint32_t* tile, Walker& q)
+{
+    if (q.k >= c.kmin) record_<AGG>(c, tile, q.k, q.de);
+    q.k = 0u;
+    q.de = 0.0f;
+}
+
+} // namespace
+
+template <bool AGG>
+__global__ void __launch_bounds__(kSplitThreads, 4) k_simulate_split(SimArgs a)
+{
+    extern __shared__ uint32_t s_tile[];
+    __shared__ uint32_t s_item, s_gmax;
+    __shared__ PropDev s_prop;
+    __shared__ JobDev s_job;
+
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    SplitShared& sh = *reinterpret_cast<SplitShared*>(s_tile + a.tile_words);
+    for (uint32_t i = tid; i < a.tile_words; i += kSplitThreads) s_tile[i] = 0u;
+    const uint32_t n_items = *a.n_items;
+    unsigned long long tasks_total = 0ull;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = atomicAdd(a.queue_head, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        if (item >= n_items) break;
+        load_item_(a, item, s_prop, s_job);
+        const ItemCtx c = item_ctx_(a, s_job, s_prop);
+        const uint32_t* prefix = a.counts + s_prop.counts_off + s_job.V; /* [V+1] */
+        const uint32_t k0 = s_job.seed_lo, k1 = s_job.seed_hi;
+        const uint32_t slot = s_prop.slot;
+        const uint32_t gt = pcs_ctr_gen_trial(s_prop.gen, s_prop.trial);
+        const uint32_t chunk_idx = item - s_prop.item_begin;
+        const uint32_t a0 = chunk_idx * a.chunk;
+        const uint32_t a1 = min(a0 + a.chunk, s_prop.total_particles);
+
+        for (uint32_t base = a0; base < a1; base += kSplitThreads) {
+            const uint32_t n = base + tid;
+            Walker q;
+            q.n = n;
+            q.F = 0u;
+            q.k = 0u;
+            q.de = 0.0f;
+            q.x = q.y = q.z = 0.0f;
+            q.sd = 0.0f;
+            q.haz = 0.0f;
+            if (n < a1) init_walker_<false>(a, c, s_job, s_prop, prefix, n, slot, gt, k0, k1, q);
+            const uint32_t steps = q.F > 0u ? q.F - 1u : 0u;
+            const uint32_t groups = (steps + 3u) >> 2;
+            if (tid == 0) {
+                s_gmax = 0u;
+                sh.count = 0u;
+            }
+            __syncthreads();
+            atomicMax(&s_gmax, groups);
+            __syncthreads();
+            const uint32_t gmax = s_gmax;
+
+            for (uint32_t g0 = 0; g0 < gmax; g0 += kSplitG) {
+                /* ---- phase Z: z per step, x, y per group, tasks queued ---- */
+                uint32_t fullmask = 0u;
+#pragma unroll 1
+                for (uint32_t gl = 0; gl < kSplitG; gl += 2u) {
+                    const uint32_t g = g0 + gl; /* even */
+                    float nz[8], ag[4];
+                    if (g < groups) {
+                        const uint32_t blk0 = 2u + 8u * (g >> 1);
+                        const pcs_u4 r0 = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, blk0));
+                        const pcs_u4 r1 = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, blk0 + 1u));
+                        const pcs_u4 r2 = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, blk0 + 2u));
+                        box_muller_(r0.x, r0.y, nz[0], nz[1]);
+                        box_muller_(r0.z, r0.w, nz[2], nz[3]);
+                        box_muller_(r1.x, r1.y, nz[4], nz[5]);
+                        box_muller_(r1.z, r1.w, nz[6], nz[7]);
+                        box_muller_(r2.x, r2.y, ag[0], ag[1]);
+                        box_muller_(r2.z, r2.w, ag[2], ag[3]);
+                    }
+#pragma unroll
+                    for (uint32_t h = 0; h < 2u; ++h) {
+                        const uint32_t gg = g + h;
+                        uint32_t zbits = 0u, m = 0u;
+                        float xs = 0.0f, ys = 0.0f, sx = 0.0f, sy = 0.0f;
+                        if (gg < groups) {
+                            m = min(4u, steps - 4u * gg);
+#pragma unroll
+                            for (uint32_t i = 0; i < 4u; ++i) {
+                                if (i < m) {
+                                    const float dz = __fmul_rn(q.sd, nz[4u * h + i]);
+                                    q.z = wrap_(__fadd_rn(q.z, dz), c.hlz, c.two_hlz);
+                                    if (fabsf(q.z) <= q.haz) zbits |= 1u << i;
+                                }
+                            }
+                            const float sds = __fmul_rn(q.sd, split_sqrt_m_(m));
+                            sx = __fmul_rn(sds, ag[2u * h]);
+                            sy = __fmul_rn(sds, ag[2u * h + 1u]);
+                            xs = q.x;
+                            ys = q.y;
+                            q.x = wrap_(__fadd_rn(q.x, sx), c.hlx, c.two_hlx);
+                            q.y = wrap_(__fadd_rn(q.y, sy), c.hly, c.two_hly);
+                        }
+                        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, zbits != 0u);
+                        if (bal) {
+                            uint32_t wbase = 0u;
+                            if (lane == 0u) wbase = atomicAdd(&sh.count, (uint32_t)__popc(bal));
+                            wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
+                            if (zbits) {
+                                const uint32_t e = wbase + (uint32_t)__popc(bal & lt_mask);
+                                sh.xs[e] = xs;
+                                sh.ys[e] = ys;
+                                sh.sx[e] = sx;
+                                sh.sy[e] = sy;
+                                sh.sd[e] = q.sd;
+                                sh.meta[e] = (tid << 16) | ((gl + h) << 8) | (m << 4) | zbits;
+                                sh.idx[gl + h][tid] = (uint16_t)e;
+                                fullmask |= 1u << (gl + h);
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+                /* ---- phase T: the queued tasks, densely ---- */
+                const uint32_t cnt = sh.count;
+                for (uint32_t e = tid; e < cnt; e += kSplitThreads) {
+                    const uint32_t meta = sh.meta[e];
+                    const uint32_t owner = meta >> 16, gl = (meta >> 8) & 0xFFu, m = (meta >> 4) & 7u;
+                    const uint32_t zbits = meta & 15u, g = g0 + gl;
+                    const float xs = sh.xs[e], ys = sh.ys[e], sxv = sh.sx[e], syv = sh.sy[e], sd = sh.sd[e];
+                    const pcs_philox_pre ph = pcs_philox_prepare(base + owner, slot, gt, k0, k1);
+                    const uint32_t blk = 2u + 8u * (g >> 1) + 3u + 2u * (g & 1u);
+                    float nx[4], ny[4];
+                    pcs_u4 r = pcs_draw_pre(ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, blk));
+                    box_muller_(r.x, r.y, nx[0], ny[0]);
+                    box_muller_(r.z, r.w, nx[1], ny[1]);
+                    r = pcs_draw_pre(ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, blk + 1u));
+                    box_muller_(r.x, r.y, nx[2], ny[2]);
+                    box_muller_(r.z, r.w, nx[3], ny[3]);
+                    const float im = split_inv_m_(m);
+                    float mx = 0.0f, my = 0.0f;
+#pragma unroll
+                    for (uint32_t i = 0; i < 4u; ++i) {
+                        if (i < m) {
+                            mx = __fadd_rn(mx, nx[i]);
+                            my = __fadd_rn(my, ny[i]);
+                        }
+                    }
+                    mx = __fmul_rn(mx, im);
+                    my = __fmul_rn(my, im);
+                    const float cx = __fmul_rn(sxv, im), cy = __fmul_rn(syv, im);
+                    float xx = xs, yy = ys, dv[4];
+                    uint32_t det = 0u;
+#pragma unroll
+                    for (uint32_t i = 0; i < 4u; ++i) {
+                        dv[i] = 0.0f;
+                        if (i < m) {
+                            const float dx = __fadd_rn(cx, __fmul_rn(sd, __fsub_rn(nx[i], mx)));
+                            const float dy = __fadd_rn(cy, __fmul_rn(sd, __fsub_rn(ny[i], my)));
+                            xx = wrap_(__fadd_rn(xx, dx), c.hlx, c.two_hlx);
+                            yy = wrap_(__fadd_rn(yy, dy), c.hly, c.two_hly);
+                            if (((zbits >> i) & 1u) && fabsf(xx) <= c.hax && fabsf(yy) <= c.hay) det |= 1u << i;
+                            dv[i] = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+                        }
+                    }
+                    sh.xs[e] = dv[0];
+                    sh.ys[e] = dv[1];
+                    sh.sx[e] = dv[2];
+                    sh.sy[e] = dv[3];
+                    sh.meta[e] = (meta & ~15u) | det;
+                }
+                tasks_total += cnt;
+                __syncthreads();
+                if (tid == 0) sh.count = 0u;
+                /* ---- phase S: track bookkeeping over this thread's groups ---- */
+                const uint32_t have = groups > g0 ? min(groups - g0, kSplitG) : 0u; /* groups of this chunk */
+                uint32_t bits = fullmask, pos = 0u;
+                while (bits) {
+                    const uint32_t gl = (uint32_t)__ffs(bits) - 1u;
+                    bits &= bits - 1u;
+                    if (gl > pos) close_track_<AGG>(c, s_tile, q); /* groups without a task before it */
+                    const uint32_t e = sh.idx[gl][tid];
+                    const uint32_t meta = sh.meta[e];
+                    const uint32_t m = (meta >> 4) & 7u;
+                    const float dv[4] = {sh.xs[e], sh.ys[e], sh.sx[e], sh.sy[e]};
+#pragma unroll
+                    for (uint32_t i = 0; i < 4u; ++i) {
+                        if (i < m) {
+                            if ((meta >> i) & 1u) {
+                                const uint32_t kp = q.k + 1u;
+                                if (kp >= 2u) q.de = __fadd_rn(q.de, dv[i]);
+                                q.k = kp;
+                            } else {
+                                close_track_<AGG>(c, s_tile, q);
+                            }
+                        }
+                    }
+                    pos = gl + 1u;
+                }
+                if (have > pos) close_track_<AGG>(c, s_tile, q); /* groups without a task after the last */
+                __syncthreads();
+            }
+            if (q.F > 0u && q.k >= c.kmin) record_<AGG>(c, s_tile, q.k, q.de);
+        }
+
+        __syncthreads();
+        /* flush the privatised rows into the proposal's histogram */
+        for (uint32_t i = tid; i < c.tile_words_used; i += kSplitThreads) {
+            const uint32_t v = s_tile[i];
+            if (v) {
+                atomicAdd(c.hist + i, v);
+                s_tile[i] = 0u;
+            }
+        }
+    }
+    if (a.tasks && tid == 0u && tasks_total) atomicAdd(a.tasks, tasks_total);
+}
+
+/* ----------------------------------------------------------------------- */
 
 namespace {
 template <int PPT, bool REPLAY, bool AGG>
@@ -338,10 +633,46 @@ int occupancy_(uint32_t block, size_t smem)
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, (int)block, smem) != cudaSuccess) return 0;
     return n;
 }
+
+template <bool AGG>
+cudaError_t launch_split_(const SimArgs& a, uint32_t grid, size_t smem, cudaStream_t st)
+{
+    auto fn = k_simulate_split<AGG>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    fn<<<grid, kSplitThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <bool AGG>
+int occupancy_split_(size_t smem)
+{
+    int n = 0;
+    auto fn = k_simulate_split<AGG>;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, (int)kSplitThreads, smem) != cudaSuccess) return 0;
+    return n;
+}
+
+/* The split walk's task queue follows the histogram tile in shared memory;
+ * the tile gives way so that both fit in 220 KB. */
+uint32_t split_tile_words_(uint32_t tile_words)
+{
+    const size_t cap = (220u * 1024u - sizeof(SplitShared)) / 4u;
+    return (uint32_t)(tile_words < cap ? tile_words : cap);
+}
 } // namespace
 
-cudaError_t launch_simulate(const SimArgs& a, const SimLaunch& l, cudaStream_t st)
+cudaError_t launch_simulate(const SimArgs& a_in, const SimLaunch& l, cudaStream_t st)
 {
+    if (l.split) {
+        if (l.replay) return cudaErrorInvalidValue;
+        SimArgs a = a_in;
+        a.tile_words = split_tile_words_(a.tile_words);
+        const size_t smem = (size_t)a.tile_words * 4u + sizeof(SplitShared);
+        return l.aggregate ? launch_split_<true>(a, l.grid, smem, st) : launch_split_<false>(a, l.grid, smem, st);
+    }
+    const SimArgs& a = a_in;
     const size_t smem = (size_t)a.tile_words * 4u;
 #define PCS_SIM_CASE(P, R, G)                                                               \
     if (l.ppt == P && l.replay == R && l.aggregate == G) return launch_sim_<P, R, G>(a, l.grid, l.block, smem, st);
@@ -359,6 +690,10 @@ cudaError_t launch_simulate(const SimArgs& a, const SimLaunch& l, cudaStream_t s
 
 int simulate_occupancy(const SimLaunch& l, uint32_t tile_words)
 {
+    if (l.split) {
+        const size_t smem = (size_t)split_tile_words_(tile_words) * 4u + sizeof(SplitShared);
+        return l.aggregate ? occupancy_split_<true>(smem) : occupancy_split_<false>(smem);
+    }
     const size_t smem = (size_t)tile_words * 4u;
 #define PCS_SIM_OCC(P, R, G) \
     if (l.ppt == P && l.replay == R && l.aggregate == G) return occupancy_<P, R, G>(l.block, smem);

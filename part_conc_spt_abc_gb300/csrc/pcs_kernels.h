@@ -36,6 +36,7 @@ struct SimArgs {
     uint32_t rp_stride;
     const float* rp_sigmas;
     uint32_t* err;
+    unsigned long long* tasks; /* nullable: slab-split walk task count (added to) */
 };
 
 struct SimLaunch {
@@ -43,6 +44,7 @@ struct SimLaunch {
     int ppt;
     bool replay;
     bool aggregate;
+    bool split; /* slab-split walk (k_simulate_split: 256 threads, 1 particle each, no replay) */
 };
 
 cudaError_t launch_simulate(const SimArgs& a, const SimLaunch& l, cudaStream_t st);

@@ -118,7 +118,11 @@ void run_plain(Job& j, uint32_t max_steps, uint32_t queues)
     sl.ppt = ref_geometry ? 1 : (int)c.tune.ppt;
     sl.replay = false;
     sl.aggregate = c.tune.aggregate == 1u;
-    const uint32_t sim_slots = ref_geometry ? (V + 3u) / 4u : c.sim_grid(sl.block, c.tune.ppt, sl.aggregate, tile_words);
+    sl.split = c.split_walk();
+    /* the split walk runs 256-thread CTAs: half as many of them give the
+     * reference geometry's thread count */
+    const uint32_t sim_slots = ref_geometry ? (sl.split ? (V + 7u) / 8u : (V + 3u) / 4u)
+                                            : c.sim_grid(sl.block, c.tune.ppt, sl.aggregate, tile_words, sl.split);
 
     JobPmcDev st = j.status; /* counters reported through pcs_job_info */
     uint64_t gen_trials = 0;

@@ -115,10 +115,17 @@ def _cfg0_setup(oracle, V=20, frames=200, parts=128, C=1):
                         np.array([1.0], np.float32), pc, rw, float(np.float32(20.0 / 100)), frames + 1, 100)
 
 
-def test_philox_forward_model_matches_oracle_streams(pcs, ctx, oracle):
-    """Same Philox streams on both sides; the GPU's fast-math Box-Muller
-    differs in the last bits, so the histograms agree to a fraction of a
-    percent, far inside Monte-Carlo noise."""
+@pytest.fixture(params=[1, 2], ids=["split", "step"])
+def walk(request, ctx):
+    ctx.set_tuning(walk=request.param)
+    yield request.param
+    ctx.set_tuning(walk=2)
+
+
+def test_philox_forward_model_matches_oracle_streams(pcs, ctx, oracle, walk):
+    """Same Philox streams on both sides, for both walks; the GPU's fast-math
+    Box-Muller differs in the last bits, so the histograms agree to a
+    fraction of a percent, far inside Monte-Carlo noise."""
     st = _cfg0_setup(oracle, C=2)
     setup, run = fwd(pcs, st)
     runs = []
@@ -127,7 +134,7 @@ def test_philox_forward_model_matches_oracle_streams(pcs, ctx, oracle):
         runs.append(r)
     got = pcs.simulate_hist(ctx, setup, runs, seed=12345)
     for s in range(4):
-        want, _ = oracle.simulate_philox(st, 12345, slot=s, trial=1, generation=2)
+        want, _ = oracle.simulate_philox(st, 12345, slot=s, trial=1, generation=2, split=walk == 1)
         tot = want.sum()
         assert tot > 1000
         assert abs(int(got[s].sum()) - int(tot)) <= 0.005 * tot + 5
@@ -142,9 +149,36 @@ def _moments(h):
     return n, (h * k).sum() / n, (h * b).sum() / n
 
 
-def test_fresh_draws_moments_within_3_se(pcs, ctx, oracle):
-    """Histogram moments of the GPU path within 3 Monte-Carlo standard errors
-    of the oracle's on independent draws at the same parameters."""
+def test_lognormal_streams_match_oracle(pcs, ctx, oracle, walk):
+    """Lognormal diameters (per-particle step sd from the size stream), both
+    walks, ragged frame counts (every partial last group, a one-frame video)."""
+    import part_conc_spt_abc_gb300.workloads as W
+    frames = np.array([80, 1, 59, 2, 130], np.uint32)
+    parts = np.array([900, 60, 750, 30, 1200], np.uint32)
+    B = 48
+    setup = W.forward_setup(frames, B, C=2)
+    sc, sh = W.lognormal_sd_params([150.0, 400.0], [15.0, 30.0])
+    pre = np.array([0.55, 2.0], np.float32)
+    runs = [pcs.ForwardRun(parts, np.array([1.0], np.float32), pre, sc, sh, slot=s, trial=2, generation=1)
+            for s in range(3)]
+    got = pcs.simulate_hist(ctx, setup, runs, seed=99)
+    st = oracle.Setup(2, 2, frames, parts, 2, setup.four_delta_t, setup.half_l, setup.half_a,
+                      np.array([1.0], np.float32), pre, np.zeros(2, np.float32), setup.dde, setup.rows, B)
+    st.ln_scale = np.array(list(sc) + [0] * 6, np.float32)
+    st.ln_shape = np.array(list(sh) + [0] * 6, np.float32)
+    for s in range(3):
+        want, _ = oracle.simulate_philox(st, 99, slot=s, trial=2, generation=1, split=walk == 1)
+        tot = want.sum()
+        assert tot > 300
+        assert abs(int(got[s].sum()) - int(tot)) <= 0.005 * tot + 5
+        assert np.abs(got[s].astype(np.int64) - want).sum() <= 0.02 * tot + 10
+
+
+def test_fresh_draws_moments_within_3_se(pcs, ctx, oracle, walk):
+    """Histogram moments of the GPU path (either walk) within 3 Monte-Carlo
+    standard errors of the oracle's per-step walk on independent draws at
+    the same parameters: for the slab-split walk this checks it against the
+    reference's step-by-step model."""
     st = _cfg0_setup(oracle)
     setup, run = fwd(pcs, st)
     reps = 24
@@ -158,7 +192,7 @@ def test_fresh_draws_moments_within_3_se(pcs, ctx, oracle):
         assert abs(a.mean() - b.mean()) <= 3 * se + 1e-9, (stat, a.mean(), b.mean(), se)
 
 
-def test_philox_determinism_and_independence(pcs, ctx, oracle):
+def test_philox_determinism_and_independence(pcs, ctx, oracle, walk):
     st = _cfg0_setup(oracle, V=5, frames=120, parts=300)
     setup, run = fwd(pcs, st)
     a = pcs.simulate_hist(ctx, setup, [run, run], seed=7)
@@ -172,7 +206,7 @@ def test_philox_determinism_and_independence(pcs, ctx, oracle):
         ctx.set_tuning(**kw)
         d = pcs.simulate_hist(ctx, setup, [run], seed=7)
         assert np.array_equal(d[0], b[0]), kw
-    ctx.set_tuning(block_size=256, particles_per_thread=1, warp_aggregate=0xFFFFFFFF)
+    ctx.set_tuning(block_size=256, particles_per_thread=1, warp_aggregate=0xFFFFFFFF, hist_tile_rows=64)
 
 
 def test_bad_arguments_raise(pcs, ctx, oracle):

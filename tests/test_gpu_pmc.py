@@ -63,7 +63,9 @@ def test_generation_invariants(pcs, ctx):
     assert info.iterations >= 2 and info.simulations > 0 and info.particle_steps > 0
 
 
-def test_results_do_not_depend_on_batching(pcs, ctx):
+@pytest.mark.parametrize("walk", [2, 1], ids=["step", "split"])
+def test_results_do_not_depend_on_batching(pcs, ctx, walk):
+    ctx.set_tuning(walk=walk)
     inp, _ = small_input(pcs, C=1, pop=64)
     fill0 = ctx.tuning.round_fill
     ref_out, ref_info = run_job(pcs, ctx, inp, 9, 3)
@@ -82,7 +84,7 @@ def test_results_do_not_depend_on_batching(pcs, ctx):
             assert info.gamma == ref_info.gamma
     finally:
         ctx.set_tuning(max_speculation=4096, block_size=256, particles_per_thread=1, hist_tile_rows=64,
-                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=fill0)
+                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=fill0, walk=2)
 
 
 @pytest.mark.parametrize("plain_launch", [1, 2], ids=["reference_launch", "persistent_grid"])

@@ -24,7 +24,16 @@ def wstats(x, w):
     return np.array([np.sum(w * x), q(0.05), q(0.95)])
 
 
-def test_posterior_matches_independent_cpu_run(pcs, ctx, oracle):
+@pytest.mark.parametrize("walk", [2, 1], ids=["step", "split"])
+def test_posterior_matches_independent_cpu_run(pcs, ctx, oracle, walk):
+    ctx.set_tuning(walk=walk)
+    try:
+        _posterior_case(pcs, ctx, oracle)
+    finally:
+        ctx.set_tuning(walk=2)
+
+
+def _posterior_case(pcs, ctx, oracle):
     import part_conc_spt_abc_gb300.workloads as W
     inp, truth = W.make_problem(ctx, [TRUTH["mu"]], [TRUTH["sd"]], TRUTH["conc_ml"] * 1e6, [1.0], 8, 80, 48, 512,
                                 GENERATIONS, seed=0, prior_mu=PRIOR["m"], prior_sd=PRIOR["s"])
