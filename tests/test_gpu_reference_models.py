@@ -76,11 +76,11 @@ def test_reference_model_generations(pcs, ctx, model, weighting):
         lc = np.log10(o.c)
         assert (lc >= np.log10(p.lb_c) - 1e-9).all() and (lc <= np.log10(p.ub_c) + 1e-9).all()
         assert o.az.shape == (N * Z,) and (o.az >= p.lb_az).all() and (o.az <= p.ub_az).all()
-        gammas.append(info.gamma)
         if done:
-            break
+            break  # the cap stops before the next decrement: the output gamma is the last one used
+        gammas.append(info.gamma)
     # delta schedule: after the prior pass, gamma drops by delta_gamma per generation
-    steps = np.diff(gammas[1:])
+    steps = np.diff(gammas)
     assert len(steps) >= 2 and np.allclose(steps, -p.delta_gamma, atol=1e-9), gammas
     assert info.iterations == p.max_generations + 1 or info.converged
     sim.close()
