@@ -254,7 +254,10 @@ pcs_status pcs_serve_submit(pcs_ctx* ctx, pcs_job* job);
 pcs_status pcs_serve_step(pcs_ctx* ctx, uint32_t* active);
 /* 1 in *finished once the job has completed. */
 pcs_status pcs_serve_poll(pcs_ctx* ctx, pcs_job* job, int* finished);
-/* Caps the device memory the serve loop may use for admitted jobs (bytes, 0 = free memory). */
+/* Caps the device memory the serve loop may use (bytes, 0 = free memory):
+ * a queued job is admitted while the admitted jobs' arenas, its own and the
+ * round histograms (round capacity x the widest admitted job's R x B words)
+ * fit; a job that does not fit even alone fails with PCS_ERR_OUT_OF_MEMORY. */
 pcs_status pcs_serve_set_memory_cap(pcs_ctx* ctx, uint64_t bytes);
 
 /* ------------------------------------------------------------------ */

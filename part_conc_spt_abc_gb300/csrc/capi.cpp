@@ -461,9 +461,16 @@ pcs_status pcs_serve_step(pcs_ctx* ctx, uint32_t* active)
             if (used >= kMaxRoundJobs) break;
             size_t free_b = 0, total_b = 0;
             PCS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            /* the job's arena plus the round histograms, which are shared and
+             * sized for the widest admitted job: capacity x max(R x B) words */
+            uint64_t rb_max = (uint64_t)j->R * j->B;
+            for (Job* t : c.table)
+                if (t) rb_max = std::max<uint64_t>(rb_max, (uint64_t)t->R * t->B);
+            const uint64_t hist_b = (uint64_t)c.tune.capacity * rb_max * 4ull;
+            const uint64_t need_total = c.mem_used + j->arena_bytes() + hist_b;
             const uint64_t need_b = j->arena_bytes() + (uint64_t)c.tune.capacity * j->R * j->B * 4ull;
-            const uint64_t limit = c.mem_cap ? (c.mem_cap > c.mem_used ? c.mem_cap - c.mem_used : 0) : (uint64_t)free_b;
-            if (need_b > limit || need_b + (64ull << 20) > (uint64_t)free_b) {
+            const bool over_cap = c.mem_cap && need_total > c.mem_cap;
+            if (over_cap || need_b + (64ull << 20) > (uint64_t)free_b) {
                 if (used == 0) throw Error(PCS_ERR_OUT_OF_MEMORY, "job does not fit in device memory");
                 break;
             }

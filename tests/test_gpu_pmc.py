@@ -138,6 +138,38 @@ def test_serve_alone_equals_mix(pcs, ctx):
         s.close()
 
 
+def test_serve_memory_cap(pcs, ctx):
+    """With a cap that holds one job's arena and the round histograms but not
+    two, jobs are admitted one after another and give the same results as
+    alone; a cap below one job's needs is an out-of-memory error."""
+    jobs = [small_input(pcs, seed=s, C=1, pop=48)[0] for s in range(2)]
+    alone = [run_job(pcs, ctx, inp, 200 + i, 1000)[0] for i, inp in enumerate(jobs)]
+    hist_b = ctx.tuning.round_capacity * (61 * 48) * 4  # 60 frames + 1 rows x 48 bins
+    cap = hist_b + 48000                                # one job's arena (32,088 B) fits, two do not
+    srv = pcs.Server(ctx, memory_cap=cap)
+    sims = [pcs.make_simulation(ctx, inp, 200 + i) for i, inp in enumerate(jobs)]
+    for s in sims:
+        srv.submit(s)
+    for _ in range(100000):
+        if srv.step() == 0:
+            break
+    for s, a in zip(sims, alone):
+        assert srv.finished(s)
+        b = s.output()
+        for f in ["m", "c", "az", "dist", "w"]:
+            assert np.array_equal(getattr(a, f), getattr(b, f)), f
+        s.close()
+    lib = pcs._lib.lib()
+    pcs._lib.check(lib.pcs_serve_set_memory_cap(ctx.h, 1 << 20), "cap")
+    srv2 = pcs.Server(ctx)
+    s = pcs.make_simulation(ctx, jobs[0], 1)
+    srv2.submit(s)
+    with pytest.raises(pcs.PcsError):
+        srv2.step()
+    s.close()
+    pcs._lib.check(lib.pcs_serve_set_memory_cap(ctx.h, 0), "cap")
+
+
 def test_inverse_distance_weights(pcs, ctx):
     inp, _ = small_input(pcs, C=1, weighting=1)
     out, info = run_job(pcs, ctx, inp, 3, 3)
