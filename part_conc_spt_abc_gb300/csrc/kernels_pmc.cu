@@ -468,7 +468,7 @@ __device__ double block_max_(double v, double* s_red)
 __device__ void start_generation_(JobPmcDev& pm)
 {
     pm.iterations += 1u;
-    if (pm.max_generations && pm.iterations > pm.max_generations) {
+    if ((pm.max_generations && pm.iterations > pm.max_generations) || pm.generation >= PCS_MAX_GENERATION) {
         pm.done = 1u;
         return;
     }

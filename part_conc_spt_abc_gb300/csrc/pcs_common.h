@@ -182,7 +182,9 @@ PCS_HD pcs_u4 pcs_draw_pre(const pcs_philox_pre& s, uint32_t c1)
     return o;
 }
 
-/* counter word 3: generation (12 bits) and trial (20 bits) */
+/* counter word 3: generation (12 bits) and trial (20 bits); a job stops
+ * before its generation counter would leave 12 bits */
+#define PCS_MAX_GENERATION 4095u
 PCS_HD uint32_t pcs_ctr_gen_trial(uint32_t gen, uint32_t trial)
 {
     return (gen << 20) | (trial & 0xFFFFFu);

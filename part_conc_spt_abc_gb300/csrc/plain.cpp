@@ -277,6 +277,7 @@ void run_plain(Job& j, uint32_t max_steps, uint32_t queues)
             /* simulation_impl.inl:202-222 */
             st.iterations += 1;
             if (j.p.max_generations && st.iterations > j.p.max_generations) break;
+            if (gen >= PCS_MAX_GENERATION) break; /* the random-stream counter holds 12 bits of generation */
             if (j.p.schedule == PCS_SCHEDULE_DELTA) gamma -= j.p.delta_gamma;
             gen += 1;
             std::partial_sum(w.begin(), w.end(), wcum.begin());
