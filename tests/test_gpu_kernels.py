@@ -61,7 +61,7 @@ def test_distance_golden_bit_exact(pcs, ctx):
 
 def test_distance_batch_and_sizes(pcs, ctx, oracle):
     rng = np.random.default_rng(8)
-    for R, B in [(301, 128), (513, 7), (1001, 256), (2, 300)]:
+    for R, B in [(301, 128), (513, 7), (1001, 256), (2, 300), (2001, 40)]:  # 2001 rows: the row-block kernel
         n = 3
         hist = rng.poisson(0.7, (n, R, B)).astype(np.uint32)
         ref = np.cumsum(np.cumsum(rng.poisson(0.7, (R, B)), 0), 1).astype(np.uint32)
