@@ -54,7 +54,7 @@ struct Tuning {
     uint32_t ppt = 1;
     uint32_t tile_rows = 64;
     uint32_t aggregate = 0;
-    uint32_t chunk = 1024;
+    uint32_t chunk = 256;
     uint32_t capacity = 2048;
     uint32_t max_spec = 4096;
     uint32_t use_graphs = 1;
