@@ -271,8 +271,16 @@ def run_serve(args, rank, world):
     import part_conc_spt_abc_gb300 as P
     import part_conc_spt_abc_gb300.workloads as W
     ctx = P.Context(rank)
+    if args.job_order:
+        ctx.set_tuning(job_order=args.job_order)
     jobs, arrivals = W.serve_stream(ctx, n_jobs=args.jobs, seed=args.seed)
-    res = {"served": serve_stream_run(P, ctx, jobs, arrivals)}
+    res = {"served": serve_stream_run(P, ctx, jobs, arrivals), "job_order": ctx.tuning.job_order}
+    if args.cmp_jobs == 0:
+        line = {"metric": "serve p50/p99 job latency, accepted proposals/s", "value": res["served"]["accepted_per_s"],
+                "unit": "accepted proposals/s", "n_gpus": 1, **res}
+        print(json.dumps(line), flush=True)
+        ctx.close()
+        return
     cmp_jobs = []
     for inp, truth, seed in jobs[:args.cmp_jobs]:
         inp.params.max_generations = args.cmp_generations
@@ -363,6 +371,8 @@ def main():
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--plain-budget", type=float, default=300.0, help="seconds allowed for each plain form")
+    ap.add_argument("--job-order", type=int, default=0, choices=[0, 1, 2],
+                    help="serve: capacity order among jobs (1 admission, 2 least remaining work; 0 library default)")
     ap.add_argument("--cmp-jobs", type=int, default=4, help="serve: jobs in the equal-work comparison")
     ap.add_argument("--cmp-generations", type=int, default=6, help="serve: generations per compared job")
     args = ap.parse_args()

@@ -62,6 +62,7 @@ class Tuning(C.Structure):
         ("warp_aggregate", C.c_uint32), ("chunk_particles", C.c_uint32), ("round_capacity", C.c_uint32),
         ("max_speculation", C.c_uint32), ("use_graphs", C.c_uint32), ("plain_launch", C.c_uint32),
         ("round_fill", C.c_uint32), ("walk", C.c_uint32),
+        ("job_order", C.c_uint32),
     ]
 
 

@@ -207,6 +207,7 @@ pcs_status pcs_get_tuning(pcs_ctx* ctx, pcs_tuning* out)
         out->plain_launch = c.tune.plain_launch;
         out->round_fill = c.tune.round_fill;
         out->walk = c.tune.walk;
+        out->job_order = c.tune.job_order;
     });
 }
 
@@ -226,7 +227,10 @@ pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t)
         }
         if (t->hist_tile_rows) c.tune.tile_rows = t->hist_tile_rows == 0xFFFFFFFFu ? 0u : t->hist_tile_rows;
         if (t->warp_aggregate) c.tune.aggregate = t->warp_aggregate == 1u ? 1u : 0u;
-        if (t->chunk_particles) c.tune.chunk = t->chunk_particles;
+        if (t->chunk_particles && t->chunk_particles != c.tune.chunk) {
+            if (!c.table.empty()) throw Error(PCS_ERR_BUSY, "the work-item size can only change with no admitted jobs");
+            c.tune.chunk = t->chunk_particles;
+        }
         if (t->round_capacity) {
             if (!c.table.empty()) throw Error(PCS_ERR_BUSY, "round capacity can only change with no admitted jobs");
             c.tune.capacity = t->round_capacity;
@@ -242,6 +246,15 @@ pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t)
         if (t->walk) {
             if (t->walk != 1u && t->walk != 2u) throw Error(PCS_ERR_INVALID_ARGUMENT, "walk must be 1 (slab-split) or 2 (per step)");
             c.tune.walk = t->walk;
+        }
+        if (t->job_order) {
+            if (t->job_order != 1u && t->job_order != 2u) throw Error(PCS_ERR_INVALID_ARGUMENT, "job_order must be 1 or 2");
+            c.tune.job_order = t->job_order;
+        }
+        /* the round plan on the device carries speculation, fill and order */
+        if (c.rb.round.p) {
+            c.upload_table();
+            PCS_CUDA(cudaStreamSynchronize(c.stream));
         }
         c.graph_dirty = true;
     });

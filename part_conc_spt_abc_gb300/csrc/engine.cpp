@@ -523,6 +523,7 @@ void Ctx::upload_table()
     r.capacity = rb.capacity;
     r.max_spec = tune.max_spec;
     r.fill = tune.round_fill;
+    r.order = tune.job_order == 2u ? 1u : 0u;
     r.chunk = tune.chunk;
     r.items_cap = rb.items_cap;
     r.counts_cap = rb.counts_cap;

@@ -103,11 +103,44 @@ __global__ void k_round_plan(PmcArgs a)
             if (a.pmc[j].generation > 0u && !a.pmc[j].done)
                 kjs[j] = (uint32_t)min((double)k, fmax((double)kjs[j], ceil((double)kjs[j] * f)));
     }
+    /* the order in which jobs take the round's capacity: admission order, or
+     * (order == 1) jobs in their prior pass first, then the least estimated
+     * remaining work first -- (pending slots + slots of the generations left)
+     * x particle-steps per proposal / acceptance rate -- which lets short
+     * jobs finish early instead of waiting behind long ones */
+    uint32_t ord[kMaxRoundJobs];
+    double key[kMaxRoundJobs];
+    const uint32_t nj = min(rd->n_jobs, kMaxRoundJobs);
+    for (uint32_t j = 0; j < nj; ++j) {
+        const JobPmcDev& pm = a.pmc[j];
+        double kv = (double)j;
+        if (rd->order == 1u && pm.generation > 0u && !pm.done) {
+            const double pacc = ((double)pm.accepted_gen + 1.0) / ((double)pm.trials + 2.0);
+            const double spp = pm.simulations ? (double)pm.particle_steps / (double)pm.simulations : 1.0;
+            const double gens_left =
+                pm.max_generations ? fmax(0.0, (double)pm.max_generations - (double)pm.iterations) : 8.0;
+            kv = 1e6 + ((double)pm.pending_count + (double)pm.N * gens_left) * spp / pacc;
+        }
+        key[j] = kv;
+        uint32_t x = j;
+        while (x > 0 && key[ord[x - 1]] > kv) {
+            ord[x] = ord[x - 1];
+            --x;
+        }
+        ord[x] = j;
+    }
+    for (uint32_t j = nj; j < rd->n_jobs; ++j) {
+        rd->job_base[j] = 0u;
+        rd->job_count[j] = 0u;
+        rd->job_k[j] = 1u;
+        rd->job_hist_base[j] = 0u;
+    }
     uint32_t base = 0;
     uint64_t hbase = 0;
-    for (uint32_t j = 0; j < rd->n_jobs; ++j) {
+    for (uint32_t o = 0; o < nj; ++o) {
+        const uint32_t j = ord[o];
         const JobPmcDev& pm = a.pmc[j];
-        const uint32_t kj = j < kMaxRoundJobs ? kjs[j] : 1u;
+        const uint32_t kj = kjs[j];
         uint64_t want = pm.done ? 0u : (uint64_t)pm.pending_count * kj;
         uint64_t room = rd->capacity - base;
         const uint64_t rb = (uint64_t)a.jobs[j].R * a.jobs[j].B;

@@ -127,7 +127,7 @@ struct RoundDev {
     uint32_t n_props;
     uint32_t n_items;
     uint32_t queue_head;
-    uint32_t pad;
+    uint32_t order;           /* capacity order: 0 admission, 1 least remaining work first */
     unsigned long long round_steps;  /* particle-steps of the round's proposals */
     unsigned long long round_cells;  /* histogram cells of the round's proposals */
     uint32_t job_base[64];    /* first proposal of each job */

@@ -73,7 +73,7 @@ def test_results_do_not_depend_on_batching(pcs, ctx, walk):
                 dict(round_capacity=200, max_speculation=64),
                 dict(max_speculation=4096, block_size=512, particles_per_thread=4, hist_tile_rows=8,
                      warp_aggregate=1),
-                dict(round_fill=0xFFFFFFFF), dict(round_fill=3000000)]
+                dict(round_fill=0xFFFFFFFF), dict(round_fill=3000000), dict(job_order=2)]
     try:
         for kw in settings:
             ctx.set_tuning(**kw)
@@ -84,7 +84,7 @@ def test_results_do_not_depend_on_batching(pcs, ctx, walk):
             assert info.gamma == ref_info.gamma
     finally:
         ctx.set_tuning(max_speculation=4096, block_size=256, particles_per_thread=1, hist_tile_rows=64,
-                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=fill0, walk=2)
+                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=fill0, walk=2, job_order=1)
 
 
 @pytest.mark.parametrize("plain_launch", [1, 2], ids=["reference_launch", "persistent_grid"])
@@ -123,19 +123,22 @@ def test_serve_alone_equals_mix(pcs, ctx):
     for i, inp in enumerate(jobs):
         out, _ = run_job(pcs, ctx, inp, 100 + i, 1000)
         alone.append(out)
-    srv = pcs.Server(ctx)
-    sims = [pcs.make_simulation(ctx, inp, 100 + i) for i, inp in enumerate(jobs)]
-    for s in sims:
-        srv.submit(s)
-    for _ in range(100000):
-        if srv.step() == 0:
-            break
-    for s, a in zip(sims, alone):
-        assert srv.finished(s)
-        b = s.output()
-        for f in ["m", "c", "az", "dist", "w"]:
-            assert np.array_equal(getattr(a, f), getattr(b, f)), f
-        s.close()
+    for order in (1, 2):  # admission order, least remaining work first
+        ctx.set_tuning(job_order=order, round_capacity=256)  # a short round: jobs compete for it
+        srv = pcs.Server(ctx)
+        sims = [pcs.make_simulation(ctx, inp, 100 + i) for i, inp in enumerate(jobs)]
+        for s in sims:
+            srv.submit(s)
+        for _ in range(100000):
+            if srv.step() == 0:
+                break
+        for s, a in zip(sims, alone):
+            assert srv.finished(s)
+            b = s.output()
+            for f in ["m", "c", "az", "dist", "w"]:
+                assert np.array_equal(getattr(a, f), getattr(b, f)), (order, f)
+            s.close()
+    ctx.set_tuning(job_order=1, round_capacity=2048)
 
 
 def test_serve_memory_cap(pcs, ctx):
