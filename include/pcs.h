@@ -160,9 +160,10 @@ typedef struct pcs_tuning {
                                    * distribution, from different draws; the autotuner never
                                    * changes it.  Replayed draws always take the per-step walk. */
     uint32_t job_order;           /* which jobs take a round's capacity first when it is short:
-                                   * 1 admission order (default), 2 jobs in their prior pass,
+                                   * 1 admission order, 2 (default) jobs in their prior pass,
                                    * then the least estimated remaining work first.  Results
-                                   * do not depend on it; latencies do. */
+                                   * do not depend on it; latencies do (64-job stream: p50
+                                   * 27 s instead of 138 s, same throughput and p99). */
 } pcs_tuning;
 pcs_status pcs_get_tuning(pcs_ctx* ctx, pcs_tuning* out);
 pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t);

@@ -61,7 +61,7 @@ struct Tuning {
     uint32_t plain_launch = 1; /* 1 reference geometry, 2 persistent grid */
     uint32_t round_fill = 0; /* particles a round is topped up to (0: none); set to one wave at open */
     uint32_t walk = 2; /* forward-model walk on Philox streams: 1 slab-split, 2 per step */
-    uint32_t job_order = 1; /* capacity order among jobs: 1 admission, 2 least remaining work first */
+    uint32_t job_order = 2; /* capacity order among jobs: 1 admission, 2 least remaining work first */
 };
 
 struct Job;

@@ -84,7 +84,7 @@ def test_results_do_not_depend_on_batching(pcs, ctx, walk):
             assert info.gamma == ref_info.gamma
     finally:
         ctx.set_tuning(max_speculation=4096, block_size=256, particles_per_thread=1, hist_tile_rows=64,
-                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=fill0, walk=2, job_order=1)
+                       warp_aggregate=0xFFFFFFFF, round_capacity=2048, round_fill=fill0, walk=2, job_order=2)
 
 
 @pytest.mark.parametrize("plain_launch", [1, 2], ids=["reference_launch", "persistent_grid"])
@@ -138,7 +138,7 @@ def test_serve_alone_equals_mix(pcs, ctx):
             for f in ["m", "c", "az", "dist", "w"]:
                 assert np.array_equal(getattr(a, f), getattr(b, f)), (order, f)
             s.close()
-    ctx.set_tuning(job_order=1, round_capacity=2048)
+    ctx.set_tuning(job_order=2, round_capacity=2048)
 
 
 def test_serve_memory_cap(pcs, ctx):
