@@ -201,15 +201,20 @@ __global__ void __launch_bounds__(1024, 1) k_distance(DistArgs a)
 
 /* Strip kernel: 16 warps, full-height strips of 32 DE columns.
  *
- * Phase A: warp w scans rows w, w+16, ... of the strip, four rows' loads in
- * flight at a time, carry per row in shared memory, zeros written back.
+ * Phase A: warp w scans rows w, w+16, ... of the strip, eight rows' loads in
+ * flight at a time (8 x 128 B per warp, 32 KB per SM at two CTAs: about the
+ * bandwidth-latency product of one SM's share of HBM), carry per row in
+ * shared memory, zeros written back.
  * Phase B: warp w scans two columns of the strip at once, c0+w for logical
  * warp w and c0+w+16 for logical warp w+16 of the reference's 32x32 launch,
  * so every lane keeps the reference's per-lane sums in two accumulators.
+ * SSD: also accumulate the exact integer sum of squares (128-bit per lane);
+ * the PMC rounds do not ask for it, the parity entry point does.
  * Two CTAs fit per SM up to ~830 rows; the tile takes R x 33 words. */
 const uint32_t kStripThreads = 512;
+const int kStripRowsInFlight = 8;
 
-template <bool F64>
+template <bool F64, bool SSD>
 __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a)
 {
     extern __shared__ uint32_t s_mem[];
@@ -247,15 +252,15 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a)
             const uint32_t c = c0 + l;
             const bool cin = c < B;
             /* phase A */
-            for (uint32_t r = w; r < R; r += 64u) {
-                uint32_t v[4];
+            for (uint32_t r = w; r < R; r += 16u * kStripRowsInFlight) {
+                uint32_t v[kStripRowsInFlight];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
+                for (int i = 0; i < kStripRowsInFlight; ++i) {
                     const uint32_t ri = r + 16u * (uint32_t)i;
                     v[i] = (ri < R && cin) ? __ldcs(hist + (uint64_t)ri * B + c) : 0u;
                 }
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
+                for (int i = 0; i < kStripRowsInFlight; ++i) {
                     const uint32_t ri = r + 16u * (uint32_t)i;
                     if (ri < R) {
                         const uint32_t cr = carry[ri];
@@ -289,8 +294,10 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a)
                     if (valid) {
                         const float ddA = __fsub_rn(__uint2float_rn(sA), __uint2float_rn(refA));
                         a2A = __fadd_rn(a2A, __fmul_rn(ddA, ddA));
-                        const uint64_t adA = (sA >= refA) ? (uint64_t)(sA - refA) : (uint64_t)(refA - sA);
-                        add128_(shi, slo, 0u, adA * adA);
+                        if (SSD) {
+                            const uint64_t adA = (sA >= refA) ? (uint64_t)(sA - refA) : (uint64_t)(refA - sA);
+                            add128_(shi, slo, 0u, adA * adA);
+                        }
                         if (F64) {
                             const double d64 = __dsub_rn((double)sA, (double)refA);
                             a2dA = __dadd_rn(a2dA, __dmul_rn(d64, d64));
@@ -299,8 +306,10 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a)
                         if (inB) {
                             const float ddB = __fsub_rn(__uint2float_rn(sB), __uint2float_rn(refB));
                             a2B = __fadd_rn(a2B, __fmul_rn(ddB, ddB));
-                            const uint64_t adB = (sB >= refB) ? (uint64_t)(sB - refB) : (uint64_t)(refB - sB);
-                            add128_(shi, slo, 0u, adB * adB);
+                            if (SSD) {
+                                const uint64_t adB = (sB >= refB) ? (uint64_t)(sB - refB) : (uint64_t)(refB - sB);
+                                add128_(shi, slo, 0u, adB * adB);
+                            }
                             if (F64) {
                                 const double d64 = __dsub_rn((double)sB, (double)refB);
                                 a2dB = __dadd_rn(a2dB, __dmul_rn(d64, d64));
@@ -326,10 +335,12 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a)
             wd0 = reduce0_(accd0);
             wd1 = reduce0_(accd1);
         }
-        for (uint32_t d = 16; d >= 1; d >>= 1) {
-            uint64_t ohi = __shfl_down_sync(0xFFFFFFFFu, shi, d);
-            uint64_t olo = __shfl_down_sync(0xFFFFFFFFu, slo, d);
-            if (l + d < 32u) add128_(shi, slo, ohi, olo);
+        if (SSD) {
+            for (uint32_t d = 16; d >= 1; d >>= 1) {
+                uint64_t ohi = __shfl_down_sync(0xFFFFFFFFu, shi, d);
+                uint64_t olo = __shfl_down_sync(0xFFFFFFFFu, slo, d);
+                if (l + d < 32u) add128_(shi, slo, ohi, olo);
+            }
         }
         if (l == 0) {
             s_tot[w] = ws0;
@@ -347,15 +358,17 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a)
             double fin64 = 0.0;
             if (F64) fin64 = reduce0_(s_tot64[l]);
             uint64_t thi = s_hi[l], tlo = s_lo[l];
-            for (uint32_t d = 16; d >= 1; d >>= 1) {
-                uint64_t ohi = __shfl_down_sync(0xFFFFFFFFu, thi, d);
-                uint64_t olo = __shfl_down_sync(0xFFFFFFFFu, tlo, d);
-                if (l + d < 32u) add128_(thi, tlo, ohi, olo);
+            if (SSD) {
+                for (uint32_t d = 16; d >= 1; d >>= 1) {
+                    uint64_t ohi = __shfl_down_sync(0xFFFFFFFFu, thi, d);
+                    uint64_t olo = __shfl_down_sync(0xFFFFFFFFu, tlo, d);
+                    if (l + d < 32u) add128_(thi, tlo, ohi, olo);
+                }
             }
             if (l == 0) {
                 a.dist_f32[p] = fin;
                 if (F64 && a.dist_f64) a.dist_f64[p] = fin64;
-                if (a.ssd) {
+                if (SSD && a.ssd) {
                     a.ssd[2 * (uint64_t)p] = thi;
                     a.ssd[2 * (uint64_t)p + 1] = tlo;
                 }
@@ -385,8 +398,8 @@ int distance_ctas_per_sm(uint32_t max_rows)
     const size_t smem = distance_smem_bytes(max_rows);
     int n = 0;
     if (use_strip(max_rows)) {
-        cudaFuncSetAttribute(k_distance_strip<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_distance_strip<false>, (int)kStripThreads, smem);
+        cudaFuncSetAttribute(k_distance_strip<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_distance_strip<false, false>, (int)kStripThreads, smem);
     } else {
         cudaFuncSetAttribute(k_distance<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_distance<false>, 1024, smem);
@@ -398,15 +411,12 @@ cudaError_t launch_distance(const DistArgs& a, uint32_t grid, cudaStream_t st)
 {
     const size_t smem = distance_smem_bytes(a.max_rows);
     if (use_strip(a.max_rows)) {
-        if (a.dist_f64) {
-            cudaError_t e = cudaFuncSetAttribute(k_distance_strip<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-            k_distance_strip<true><<<grid, kStripThreads, smem, st>>>(a);
-        } else {
-            cudaError_t e = cudaFuncSetAttribute(k_distance_strip<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-            k_distance_strip<false><<<grid, kStripThreads, smem, st>>>(a);
-        }
+        void (*k)(DistArgs);
+        if (a.dist_f64) k = a.ssd ? k_distance_strip<true, true> : k_distance_strip<true, false>;
+        else k = a.ssd ? k_distance_strip<false, true> : k_distance_strip<false, false>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<grid, kStripThreads, smem, st>>>(a);
         return cudaGetLastError();
     }
     if (a.dist_f64) {

@@ -59,17 +59,23 @@ def test_distance_golden_bit_exact(pcs, ctx):
         assert r["ssd"][0] == (int(hi) << 64) | int(lo), i
 
 
-def test_distance_batch_and_sizes(pcs, ctx, oracle):
+@pytest.mark.parametrize("want_f64,want_ssd", [(False, True), (False, False), (True, False), (True, True)])
+def test_distance_batch_and_sizes(pcs, ctx, oracle, want_f64, want_ssd):
+    """Every kernel variant (with and without the double and exact-integer sums,
+    which the PMC rounds leave out) gives the oracle's float distance."""
     rng = np.random.default_rng(8)
     for R, B in [(301, 128), (513, 7), (1001, 256), (2, 300), (2001, 40)]:  # 2001 rows: the row-block kernel
         n = 3
         hist = rng.poisson(0.7, (n, R, B)).astype(np.uint32)
         ref = np.cumsum(np.cumsum(rng.poisson(0.7, (R, B)), 0), 1).astype(np.uint32)
-        r = pcs.scan_distance(ctx, hist, ref, want_ssd=True)
+        r = pcs.scan_distance(ctx, hist, ref, want_f64=want_f64, want_ssd=want_ssd)
         for q in range(n):
             d, _, ssd = oracle.distance_kdist(hist[q], ref)
             assert r["dist_f32"][q].tobytes() == np.float32(d).tobytes(), (R, B, q)
-            assert r["ssd"][q] == ssd
+            if want_ssd:
+                assert r["ssd"][q] == ssd
+            if want_f64:
+                assert r["dist_f64"][q] == oracle.distance_kdist_f64(hist[q], ref), (R, B, q)
 
 
 def test_observed_sat_matches_oracle(pcs, ctx, oracle):
