@@ -4,22 +4,25 @@
  * Follows cusim::K_distance (src/gpu/cusim/kernel-distance.inl:81-241), which
  * runs one 32x32 block per proposal over the whole R x B histogram twice
  * (row scans, then column scans accumulating (cum - ref)^2) and zeroes the
- * histogram for reuse.  Here one 1024-thread CTA per proposal streams the
- * histogram in strips of 32 DE columns and blocks of rows through shared
- * memory:
- *   phase A  warp w scans rows w, w+32, ... of the strip (coalesced 128-byte
- *            loads, warp shuffle scan, per-row carry across strips kept in
- *            shared memory) and writes zeros back;
- *   phase B  warp w scans column c0+w down the rows (shuffle scan, carry in a
- *            register), reads the observed cumulative histogram from its
- *            transposed copy (coalesced), and lane l accumulates
- *            (float(cum) - float(ref))^2 for rows l, l+32, ...
+ * histogram for reuse.  Here one CTA per proposal streams the histogram in
+ * strips of 32 DE columns through a shared-memory tile (row pitch 33 words,
+ * so row-wise and column-wise accesses are both conflict-free):
+ *   k_distance_strip (up to ~1650 rows, 512 threads): the whole strip
+ *            height sits in the tile; phase A builds its 2-D prefix sums
+ *            (coalesced 128-byte loads, zeros written back, per-lane column
+ *            and row passes, per-row carry across strips in shared memory),
+ *            phase B
+ *            reads column c0+w for logical warp w while lane l accumulates
+ *            (float(cum) - float(ref))^2 for rows l, l+32, ..., the observed
+ *            cumulative histogram read from its transposed copy (coalesced);
+ *   k_distance (taller histograms, 1024 threads): the same in blocks of
+ *            256 rows, with the column carry in a register.
  * Warp w / lane l therefore own exactly the columns and rows they own in the
  * reference launch, so the per-lane sums, the shfl_down trees of reduce0
  * (:69-78) and the final per-warp tree reproduce the reference's float
  * result bit for bit (each operation is an explicit round-to-nearest
  * intrinsic, as in a build without FMA contraction).  The exact integer sum
- * of squares is accumulated alongside.
+ * of squares and a double-precision sum are accumulated alongside on request.
  */
 #include <cuda_runtime.h>
 
@@ -199,122 +202,199 @@ __global__ void __launch_bounds__(1024, 1) k_distance(DistArgs a)
     }
 }
 
-/* Strip kernel: 16 warps, full-height strips of 32 DE columns.
+/* Strip kernel: 16 warps, full-height strips of 32 DE columns, a persistent
+ * CTA walking the (proposal, strip) sequence blockIdx.x, blockIdx.x + grid,
+ * ... strip by strip.
  *
- * Phase A: warp w scans rows w, w+16, ... of the strip, eight rows' loads in
- * flight at a time (8 x 128 B per warp, 32 KB per SM at two CTAs: about the
- * bandwidth-latency product of one SM's share of HBM), carry per row in
- * shared memory, zeros written back.
- * Phase B: warp w scans two columns of the strip at once, c0+w for logical
- * warp w and c0+w+16 for logical warp w+16 of the reference's 32x32 launch,
- * so every lane keeps the reference's per-lane sums in two accumulators.
+ * Copy: warp w owns a contiguous segment of ceil(R/16) rows; lane l copies
+ * column c0+l of those rows into the tile with 4-byte cp.async (any B, any
+ * offset; columns past B are zero-filled).  With two tiles (db) the copies of
+ * the next strip -- or of the next proposal's first strip -- are in flight
+ * while the current strip is computed, so the histogram streams from HBM
+ * without a round trip per strip; with one tile (tall histograms) the copies
+ * of a strip are issued together, one round trip per strip.
+ * Phase A1: each lane sums its own copied cells (column totals of the
+ * segment) and writes zeros back to the histogram, as K_distance does.
+ * Phase A2: lane l runs down column c0+l of the segment from the totals of
+ * the segments above (column prefix), then lane j runs across row rb+j from
+ * the row's carry of the strips to its left (row prefix): the tile holds the
+ * 2-D prefix sums after per-lane chains through shared memory, no shuffles
+ * (the 33-word pitch keeps both passes free of bank conflicts).
+ * Phase B: warp w reads two columns of the strip, c0+w for logical warp w
+ * and c0+w+16 for logical warp w+16 of the reference's 32x32 launch, so
+ * every lane keeps the reference's per-lane sums in two accumulators; the
+ * observed cumulative histogram of four 32-row groups is requested at once.
  * SSD: also accumulate the exact integer sum of squares (128-bit per lane);
  * the PMC rounds do not ask for it, the parity entry point does.
- * Two CTAs fit per SM up to ~830 rows; the tile takes R x 33 words. */
+ * R x 33 words per tile: two tiles and two CTAs per SM up to ~420 rows. */
 const uint32_t kStripThreads = 512;
-const int kStripRowsInFlight = 8;
+const int kStripRefGroups = 4;
+
+__device__ __forceinline__ void cp_async4_(uint32_t* dst, const uint32_t* src, bool valid)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int n = valid ? 4 : 0; /* 0: the destination is zero-filled, src is not read */
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit_() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait_() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+/* Issue this lane's copies of strip c0 of proposal p into tile T. */
+__device__ __forceinline__ void strip_copy_(const DistArgs& a, uint32_t p, uint32_t c0, uint32_t* T, uint32_t w,
+                                            uint32_t l)
+{
+    const uint32_t job = a.props[p].job;
+    const uint32_t R = a.jobs[job].R, B = a.jobs[job].B;
+    if (R > a.max_rows) return;
+    const uint32_t* hist = a.hist + a.props[p].hist_off;
+    const uint32_t seg = (R + 15u) / 16u;
+    const uint32_t rb = min(R, w * seg), re = min(R, rb + seg);
+    const uint32_t c = c0 + l;
+    const bool cin = c < B;
+    for (uint32_t r = rb; r < re; ++r) cp_async4_(T + r * kPad + l, cin ? hist + (uint64_t)r * B + c : hist, cin);
+}
 
 template <bool F64, bool SSD>
-__global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a)
+__global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t db)
 {
     extern __shared__ uint32_t s_mem[];
-    uint32_t* carry = s_mem;            /* [max_rows] */
-    uint32_t* T = s_mem + a.max_rows;   /* [max_rows][kPad] */
+    uint32_t* carry = s_mem;                              /* [max_rows] */
+    uint32_t* tiles = s_mem + a.max_rows;                 /* [1 + db][max_rows][kPad] */
+    const uint32_t tile_words = a.max_rows * kPad;
     __shared__ float s_tot[32];
     __shared__ double s_tot64[32];
     __shared__ uint64_t s_hi[32], s_lo[32];
+    __shared__ uint32_t s_col[16][32]; /* column totals of each warp's row segment */
 
     const uint32_t tid = threadIdx.x;
     const uint32_t w = tid >> 5, l = tid & 31u;
     const uint32_t M = *a.n_props;
+    uint32_t p = blockIdx.x;
+    if (p >= M) return;
 
-    for (uint32_t p = blockIdx.x; p < M; p += gridDim.x) {
+    uint32_t c0 = 0, cur = 0;
+    strip_copy_(a, p, 0u, tiles, w, l);
+    cp_async_commit_();
+
+    float acc0 = 0.0f, acc1 = 0.0f;
+    double accd0 = 0.0, accd1 = 0.0;
+    uint64_t shi = 0, slo = 0;
+    for (;;) {
         const uint32_t job = a.props[p].job;
         const uint64_t hoff = a.props[p].hist_off;
         const uint32_t R = a.jobs[job].R, B = a.jobs[job].B;
-        const uint32_t* __restrict__ refT = a.jobs[job].ref_sat_t;
-        uint32_t* hist = a.hist + hoff;
-        uint32_t* cum = a.cum_out ? a.cum_out + hoff : nullptr;
-        if (R > a.max_rows) {
+        const bool ok = R <= a.max_rows;
+        /* the (proposal, strip) after this one */
+        uint32_t pn = p, cn = c0 + 32u;
+        if (!ok || cn >= B) {
+            pn = p + gridDim.x;
+            cn = 0u;
+        }
+        const bool has_next = pn < M;
+        if (db) {
+            if (has_next) strip_copy_(a, pn, cn, tiles + (cur ^ 1u) * tile_words, w, l);
+            cp_async_commit_();
+            cp_async_wait_<1>(); /* this lane's copies of the current strip have landed */
+        } else {
+            cp_async_wait_<0>();
+        }
+        uint32_t* T = tiles + cur * tile_words;
+
+        if (!ok) {
             if (tid == 0) {
                 atomicOr(a.err, PCS_ERRBIT_ROWS);
                 a.dist_f32[p] = __int_as_float(0x7fc00000);
             }
-            continue;
-        }
-        for (uint32_t r = tid; r < R; r += kStripThreads) carry[r] = 0u;
-        __syncthreads();
-
-        float acc0 = 0.0f, acc1 = 0.0f;
-        double accd0 = 0.0, accd1 = 0.0;
-        uint64_t shi = 0, slo = 0;
-        for (uint32_t c0 = 0; c0 < B; c0 += 32u) {
+        } else {
+            const uint32_t* __restrict__ refT = a.jobs[job].ref_sat_t;
+            uint32_t* hist = a.hist + hoff;
+            uint32_t* cum = a.cum_out ? a.cum_out + hoff : nullptr;
+            const uint32_t seg = (R + 15u) / 16u;
+            const uint32_t rb = min(R, w * seg), re = min(R, rb + seg);
             const uint32_t c = c0 + l;
             const bool cin = c < B;
-            /* phase A */
-            for (uint32_t r = w; r < R; r += 16u * kStripRowsInFlight) {
-                uint32_t v[kStripRowsInFlight];
+            /* phase A1: this lane's cells -> column total, zeros written back */
+            uint32_t coltot = 0u;
+#pragma unroll 4
+            for (uint32_t r = rb; r < re; ++r) {
+                coltot += T[r * kPad + l];
+                if (cin) __stcs(hist + (uint64_t)r * B + c, 0u);
+            }
+            s_col[w][l] = coltot;
+            __syncthreads();
+            /* phase A2: column prefix down the segment, then row prefix across
+             * the strip: the tile holds the 2-D prefix sums */
+            uint32_t run = 0u;
+            for (uint32_t q = 0; q < w; ++q) run += s_col[q][l];
+#pragma unroll 4
+            for (uint32_t r = rb; r < re; ++r) {
+                run += T[r * kPad + l];
+                T[r * kPad + l] = run;
+            }
+            __syncwarp();
+            for (uint32_t r = rb + l; r < re; r += 32u) {
+                uint32_t* row = T + r * kPad;
+                uint32_t v[32];
 #pragma unroll
-                for (int i = 0; i < kStripRowsInFlight; ++i) {
-                    const uint32_t ri = r + 16u * (uint32_t)i;
-                    v[i] = (ri < R && cin) ? __ldcs(hist + (uint64_t)ri * B + c) : 0u;
-                }
+                for (int j = 0; j < 32; ++j) v[j] = row[j];
+                uint32_t acc = c0 ? carry[r] : 0u;
 #pragma unroll
-                for (int i = 0; i < kStripRowsInFlight; ++i) {
-                    const uint32_t ri = r + 16u * (uint32_t)i;
-                    if (ri < R) {
-                        const uint32_t cr = carry[ri];
-                        const uint32_t s = warp_scan_(v[i], l) + cr;
-                        T[ri * kPad + l] = s;
-                        if (cin) __stcs(hist + (uint64_t)ri * B + c, 0u);
-                        __syncwarp();
-                        if (l == 31u) carry[ri] = s;
-                    }
+                for (int j = 0; j < 32; ++j) {
+                    acc += v[j];
+                    row[j] = acc;
                 }
+                carry[r] = acc;
             }
             __syncthreads();
             /* phase B: columns c0 + w and c0 + w + 16 */
             const uint32_t colA = c0 + w, colB = c0 + w + 16u;
             const bool inA = colA < B, inB = colB < B;
-            uint32_t carA = 0u, carB = 0u;
-            float a2A = 0.0f, a2B = 0.0f;
-            double a2dA = 0.0, a2dB = 0.0;
             if (inA) {
-                for (uint32_t r0 = 0; r0 < R; r0 += 32u) {
-                    const uint32_t r = r0 + l;
-                    const bool valid = r < R;
-                    const uint32_t vA = valid ? T[r * kPad + w] : 0u;
-                    const uint32_t vB = (valid && inB) ? T[r * kPad + w + 16u] : 0u;
-                    const uint32_t refA = valid ? __ldg(refT + (uint64_t)colA * R + r) : 0u;
-                    const uint32_t refB = (valid && inB) ? __ldg(refT + (uint64_t)colB * R + r) : 0u;
-                    const uint32_t sA = warp_scan_(vA, l) + carA;
-                    const uint32_t sB = warp_scan_(vB, l) + carB;
-                    carA = __shfl_sync(0xFFFFFFFFu, sA, 31);
-                    carB = __shfl_sync(0xFFFFFFFFu, sB, 31);
-                    if (valid) {
-                        const float ddA = __fsub_rn(__uint2float_rn(sA), __uint2float_rn(refA));
-                        a2A = __fadd_rn(a2A, __fmul_rn(ddA, ddA));
-                        if (SSD) {
-                            const uint64_t adA = (sA >= refA) ? (uint64_t)(sA - refA) : (uint64_t)(refA - sA);
-                            add128_(shi, slo, 0u, adA * adA);
-                        }
-                        if (F64) {
-                            const double d64 = __dsub_rn((double)sA, (double)refA);
-                            a2dA = __dadd_rn(a2dA, __dmul_rn(d64, d64));
-                        }
-                        if (cum) cum[(uint64_t)r * B + colA] = sA;
-                        if (inB) {
-                            const float ddB = __fsub_rn(__uint2float_rn(sB), __uint2float_rn(refB));
-                            a2B = __fadd_rn(a2B, __fmul_rn(ddB, ddB));
+                float a2A = 0.0f, a2B = 0.0f;
+                double a2dA = 0.0, a2dB = 0.0;
+                for (uint32_t rg = 0; rg < R; rg += 32u * kStripRefGroups) {
+                    uint32_t refAv[kStripRefGroups], refBv[kStripRefGroups];
+#pragma unroll
+                    for (int g = 0; g < kStripRefGroups; ++g) {
+                        const uint32_t r = rg + 32u * (uint32_t)g + l;
+                        refAv[g] = r < R ? __ldg(refT + (uint64_t)colA * R + r) : 0u;
+                        refBv[g] = (r < R && inB) ? __ldg(refT + (uint64_t)colB * R + r) : 0u;
+                    }
+#pragma unroll
+                    for (int g = 0; g < kStripRefGroups; ++g) {
+                        const uint32_t r = rg + 32u * (uint32_t)g + l;
+                        if (r < R) {
+                            const uint32_t sA = T[r * kPad + w];
+                            const uint32_t refA = refAv[g];
+                            const float ddA = __fsub_rn(__uint2float_rn(sA), __uint2float_rn(refA));
+                            a2A = __fadd_rn(a2A, __fmul_rn(ddA, ddA));
                             if (SSD) {
-                                const uint64_t adB = (sB >= refB) ? (uint64_t)(sB - refB) : (uint64_t)(refB - sB);
-                                add128_(shi, slo, 0u, adB * adB);
+                                const uint64_t adA = (sA >= refA) ? (uint64_t)(sA - refA) : (uint64_t)(refA - sA);
+                                add128_(shi, slo, 0u, adA * adA);
                             }
                             if (F64) {
-                                const double d64 = __dsub_rn((double)sB, (double)refB);
-                                a2dB = __dadd_rn(a2dB, __dmul_rn(d64, d64));
+                                const double d64 = __dsub_rn((double)sA, (double)refA);
+                                a2dA = __dadd_rn(a2dA, __dmul_rn(d64, d64));
                             }
-                            if (cum) cum[(uint64_t)r * B + colB] = sB;
+                            if (cum) cum[(uint64_t)r * B + colA] = sA;
+                            if (inB) {
+                                const uint32_t sB = T[r * kPad + w + 16u];
+                                const uint32_t refB = refBv[g];
+                                const float ddB = __fsub_rn(__uint2float_rn(sB), __uint2float_rn(refB));
+                                a2B = __fadd_rn(a2B, __fmul_rn(ddB, ddB));
+                                if (SSD) {
+                                    const uint64_t adB = (sB >= refB) ? (uint64_t)(sB - refB) : (uint64_t)(refB - sB);
+                                    add128_(shi, slo, 0u, adB * adB);
+                                }
+                                if (F64) {
+                                    const double d64 = __dsub_rn((double)sB, (double)refB);
+                                    a2dB = __dadd_rn(a2dB, __dmul_rn(d64, d64));
+                                }
+                                if (cum) cum[(uint64_t)r * B + colB] = sB;
+                            }
                         }
                     }
                 }
@@ -325,69 +405,89 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a)
                     if (F64) accd1 = __dadd_rn(accd1, a2dB);
                 }
             }
-            __syncthreads();
         }
+        __syncthreads(); /* the tile is free for the copies issued next */
 
-        /* reduce0 per logical warp (w and w + 16), then over the 32 totals */
-        const float ws0 = reduce0_(acc0), ws1 = reduce0_(acc1);
-        double wd0 = 0.0, wd1 = 0.0;
-        if (F64) {
-            wd0 = reduce0_(accd0);
-            wd1 = reduce0_(accd1);
-        }
-        if (SSD) {
-            for (uint32_t d = 16; d >= 1; d >>= 1) {
-                uint64_t ohi = __shfl_down_sync(0xFFFFFFFFu, shi, d);
-                uint64_t olo = __shfl_down_sync(0xFFFFFFFFu, slo, d);
-                if (l + d < 32u) add128_(shi, slo, ohi, olo);
+        if (ok && c0 + 32u >= B) {
+            /* last strip: reduce0 per logical warp (w and w + 16), then over
+             * the 32 totals */
+            const float ws0 = reduce0_(acc0), ws1 = reduce0_(acc1);
+            double wd0 = 0.0, wd1 = 0.0;
+            if (F64) {
+                wd0 = reduce0_(accd0);
+                wd1 = reduce0_(accd1);
             }
-        }
-        if (l == 0) {
-            s_tot[w] = ws0;
-            s_tot[w + 16] = ws1;
-            s_tot64[w] = wd0;
-            s_tot64[w + 16] = wd1;
-            s_hi[w] = shi;
-            s_lo[w] = slo;
-            s_hi[w + 16] = 0u;
-            s_lo[w + 16] = 0u;
-        }
-        __syncthreads();
-        if (w == 0) {
-            const float fin = reduce0_(s_tot[l]);
-            double fin64 = 0.0;
-            if (F64) fin64 = reduce0_(s_tot64[l]);
-            uint64_t thi = s_hi[l], tlo = s_lo[l];
             if (SSD) {
                 for (uint32_t d = 16; d >= 1; d >>= 1) {
-                    uint64_t ohi = __shfl_down_sync(0xFFFFFFFFu, thi, d);
-                    uint64_t olo = __shfl_down_sync(0xFFFFFFFFu, tlo, d);
-                    if (l + d < 32u) add128_(thi, tlo, ohi, olo);
+                    uint64_t ohi = __shfl_down_sync(0xFFFFFFFFu, shi, d);
+                    uint64_t olo = __shfl_down_sync(0xFFFFFFFFu, slo, d);
+                    if (l + d < 32u) add128_(shi, slo, ohi, olo);
                 }
             }
             if (l == 0) {
-                a.dist_f32[p] = fin;
-                if (F64 && a.dist_f64) a.dist_f64[p] = fin64;
-                if (SSD && a.ssd) {
-                    a.ssd[2 * (uint64_t)p] = thi;
-                    a.ssd[2 * (uint64_t)p + 1] = tlo;
+                s_tot[w] = ws0;
+                s_tot[w + 16] = ws1;
+                s_tot64[w] = wd0;
+                s_tot64[w + 16] = wd1;
+                s_hi[w] = shi;
+                s_lo[w] = slo;
+                s_hi[w + 16] = 0u;
+                s_lo[w + 16] = 0u;
+            }
+            __syncthreads();
+            if (w == 0) {
+                const float fin = reduce0_(s_tot[l]);
+                double fin64 = 0.0;
+                if (F64) fin64 = reduce0_(s_tot64[l]);
+                uint64_t thi = s_hi[l], tlo = s_lo[l];
+                if (SSD) {
+                    for (uint32_t d = 16; d >= 1; d >>= 1) {
+                        uint64_t ohi = __shfl_down_sync(0xFFFFFFFFu, thi, d);
+                        uint64_t olo = __shfl_down_sync(0xFFFFFFFFu, tlo, d);
+                        if (l + d < 32u) add128_(thi, tlo, ohi, olo);
+                    }
+                }
+                if (l == 0) {
+                    a.dist_f32[p] = fin;
+                    if (F64 && a.dist_f64) a.dist_f64[p] = fin64;
+                    if (SSD && a.ssd) {
+                        a.ssd[2 * (uint64_t)p] = thi;
+                        a.ssd[2 * (uint64_t)p + 1] = tlo;
+                    }
                 }
             }
+            __syncthreads();
+            acc0 = acc1 = 0.0f;
+            accd0 = accd1 = 0.0;
+            shi = slo = 0u;
         }
-        __syncthreads();
+        if (!has_next) break;
+        if (!db) {
+            strip_copy_(a, pn, cn, tiles, w, l);
+            cp_async_commit_();
+        } else {
+            cur ^= 1u;
+        }
+        p = pn;
+        c0 = cn;
     }
+    cp_async_wait_<0>();
 }
 
-static size_t strip_smem_bytes(uint32_t max_rows)
+static const size_t kStripSmemMax = 220u * 1024u;
+
+/* carry + one or two tiles */
+static size_t strip_smem_bytes(uint32_t max_rows, bool db)
 {
-    return ((size_t)max_rows * (1u + kPad)) * sizeof(uint32_t);
+    return ((size_t)max_rows * (1u + (db ? 2u : 1u) * kPad)) * sizeof(uint32_t);
 }
 
-static bool use_strip(uint32_t max_rows) { return strip_smem_bytes(max_rows) <= 220u * 1024u; }
+static bool use_strip(uint32_t max_rows) { return strip_smem_bytes(max_rows, false) <= kStripSmemMax; }
+static bool strip_db(uint32_t max_rows) { return strip_smem_bytes(max_rows, true) <= kStripSmemMax; }
 
 size_t distance_smem_bytes(uint32_t max_rows)
 {
-    if (use_strip(max_rows)) return strip_smem_bytes(max_rows);
+    if (use_strip(max_rows)) return strip_smem_bytes(max_rows, strip_db(max_rows));
     return ((size_t)max_rows + (size_t)kDistRowBlock * kPad) * sizeof(uint32_t);
 }
 
@@ -411,12 +511,12 @@ cudaError_t launch_distance(const DistArgs& a, uint32_t grid, cudaStream_t st)
 {
     const size_t smem = distance_smem_bytes(a.max_rows);
     if (use_strip(a.max_rows)) {
-        void (*k)(DistArgs);
+        void (*k)(DistArgs, uint32_t);
         if (a.dist_f64) k = a.ssd ? k_distance_strip<true, true> : k_distance_strip<true, false>;
         else k = a.ssd ? k_distance_strip<false, true> : k_distance_strip<false, false>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k<<<grid, kStripThreads, smem, st>>>(a);
+        k<<<grid, kStripThreads, smem, st>>>(a, strip_db(a.max_rows) ? 1u : 0u);
         return cudaGetLastError();
     }
     if (a.dist_f64) {
