@@ -165,10 +165,50 @@ __global__ void k_round_plan(PmcArgs a)
 }
 
 /* ----------------------------------------------------------------------- */
-/* one warp per proposal: lane 0 builds the parameters and forward-model
- * arguments (FP64), the lanes draw the per-video Poisson counts in parallel
- * (each count has its own Philox counter, so the counts equal
- * pcs_draw_counts') and scan them into the video prefix. */
+/* First index i < N with !(wcum[i] < u) (std::lower_bound on a
+ * non-decreasing array), clamped to N - 1, as pcs_pick: a 32-way search, each
+ * lane probing one split point per round (2 dependent loads for N = 1024
+ * instead of 10). */
+__device__ __forceinline__ uint32_t warp_pick_(const double* wcum, uint32_t N, double u, uint32_t lane)
+{
+    uint32_t lo = 0, hi = N; /* the answer lies in [lo, hi]; hi == N: none found yet */
+    for (int round = 0; round < 8 && hi > lo; ++round) {
+        const uint32_t span = hi - lo;
+        uint32_t idx;
+        bool valid;
+        if (span <= 32u) {
+            idx = lo + lane;
+            valid = lane < span;
+        } else {
+            idx = lo + (uint32_t)(((uint64_t)(lane + 1u) * span) / 32u) - 1u;
+            valid = true;
+        }
+        const bool ge = valid && !(wcum[idx] < u);
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, ge);
+        if (m == 0u) {
+            lo = hi;
+            break;
+        }
+        const uint32_t f = (uint32_t)(__ffs(m) - 1);
+        const uint32_t idx_f = __shfl_sync(0xFFFFFFFFu, idx, f);
+        if (span <= 32u) {
+            lo = hi = idx_f;
+            break;
+        }
+        const uint32_t prev = __shfl_sync(0xFFFFFFFFu, idx, f > 0u ? f - 1u : 0u);
+        lo = f > 0u ? prev + 1u : lo;
+        hi = idx_f;
+    }
+    return lo < N ? lo : N - 1u;
+}
+
+/* One warp per proposal.  The FP64 work is spread over the lanes: lane i
+ * draws perturbation normal pair i, lane p perturbs and reflects parameter p,
+ * lane c computes component c's arguments (10^log10c, step sd); the Poisson
+ * constants are computed once and the lanes draw the per-video counts in
+ * parallel (each count has its own Philox counter) and scan them into the
+ * video prefix.  Every value is the one pcs_build_theta / pcs_build_args /
+ * pcs_draw_counts compute (same functions, same operation order). */
 constexpr uint32_t kProposeWarps = 8;
 
 __global__ void __launch_bounds__(32 * kProposeWarps) k_propose(PmcArgs a)
@@ -187,34 +227,68 @@ __global__ void __launch_bounds__(32 * kProposeWarps) k_propose(PmcArgs a)
     const uint32_t trial = pm.next_trial[slot] + rep;
     const uint32_t gen = pm.generation;
     const uint32_t k0 = jd.seed_lo, k1 = jd.seed_hi;
+    const uint32_t P = pm.P;
+    const uint32_t gt = pcs_ctr_gen_trial(gen, trial);
 
-    PropDev pd;
-    double lambda = 0.0;
-    if (lane == 0u) {
-        double th[PCS_MAX_P];
-        pcs_build_theta(pm, pm.theta, pm.wcum, pm.factor, slot, trial, gen, k0, k1, th);
-        double* out = a.theta_prop + (uint64_t)q * PCS_MAX_P;
-        for (uint32_t p = 0; p < pm.P; ++p) out[p] = th[p];
-        pd.job = j;
-        pd.slot = slot;
-        pd.trial = trial;
-        pd.gen = gen;
-        pd.quirk_full_az = 0u;
-        lambda = pcs_build_args(pm, th, gen, pd);
+    /* parameters: lane p holds parameter p */
+    double th_l = 0.0;
+    if (gen == 0u) {
+        if (lane < P) th_l = pm.theta[(uint64_t)slot * P + lane];
+    } else {
+        const pcs_u4 r = pcs_draw(0u, pcs_ctr_tag(PCS_STREAM_PICK, 0u), slot, gt, k0, k1);
+        const uint32_t parent = warp_pick_(pm.wcum, pm.N, pcs_u01_53(r.x, r.y), lane);
+        const double* tp = pm.theta + (uint64_t)parent * P;
+        double n0 = 0.0, n1 = 0.0;
+        if (2u * lane < P) {
+            const pcs_u4 rr = pcs_draw(lane, pcs_ctr_tag(PCS_STREAM_PERTURB, 0u), slot, gt, k0, k1);
+            pcs_normal2(rr, n0, n1);
+        }
+        double nrm[PCS_MAX_P];
+        for (uint32_t i = 0; i < P; ++i) { /* P is the same on every lane */
+            const double a0 = __shfl_sync(0xFFFFFFFFu, n0, i >> 1);
+            const double a1 = __shfl_sync(0xFFFFFFFFu, n1, i >> 1);
+            nrm[i] = (i & 1u) ? a1 : a0;
+        }
+        if (lane < P) th_l = pcs_perturb_one(pm, tp, pm.factor, nrm, lane);
     }
-    lambda = __shfl_sync(0xFFFFFFFFu, lambda, 0);
+    double th[PCS_MAX_P];
+    for (uint32_t i = 0; i < P; ++i) th[i] = __shfl_sync(0xFFFFFFFFu, th_l, i);
+    if (gen != 0u) pcs_sort_components(pm, th);
 
+    /* per-component arguments: lane c computes component c */
+    CompArgs ca_l;
+    ca_l.powc = 0.0;
+    ca_l.sd_scale = ca_l.sd_shape = 0.0f;
+    if (lane < pm.C) ca_l = pcs_comp_args(pm, th, lane);
+    CompArgs ca[PCS_MAX_C];
+    for (uint32_t i = 0; i < pm.C; ++i) {
+        ca[i].powc = __shfl_sync(0xFFFFFFFFu, ca_l.powc, i);
+        ca[i].sd_scale = __shfl_sync(0xFFFFFFFFu, ca_l.sd_scale, i);
+        ca[i].sd_shape = __shfl_sync(0xFFFFFFFFu, ca_l.sd_shape, i);
+    }
+    PropDev pd;
+    pd.job = j;
+    pd.slot = slot;
+    pd.trial = trial;
+    pd.gen = gen;
+    pd.quirk_full_az = 0u;
+    const double lambda = pcs_assemble_args(pm, th, ca, gen, pd);
+    if (lane == 0u) {
+        double* out = a.theta_prop + (uint64_t)q * PCS_MAX_P;
+        for (uint32_t p = 0; p < P; ++p) out[p] = th[p];
+    }
+
+    const PoissonSetup ps = pcs_poisson_setup(lambda);
     const uint64_t coff = (uint64_t)q * (2u * rd->v_max + 1u);
     uint32_t* cnt = a.counts + coff;
     uint32_t* pre = cnt + jd.V;
-    const uint32_t gt = pcs_ctr_gen_trial(gen, trial);
     uint64_t run = 0, steps = 0;
     if (lane == 0u) pre[0] = 0u;
     for (uint32_t v0 = 0; v0 < jd.V; v0 += 32u) {
         const uint32_t v = v0 + lane;
         uint32_t c = 0u;
         if (v < jd.V) {
-            c = pcs_poisson(lambda, v, slot, gt, k0, k1);
+            c = pcs_poisson_draw(ps, v, slot, gt, k0, k1);
             cnt[v] = c;
             steps += (uint64_t)c * jd.frames[v];
         }

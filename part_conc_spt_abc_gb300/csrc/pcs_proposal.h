@@ -72,14 +72,42 @@ PCS_HD double pcs_reflect(double bis, double lo, double hi)
 
 /* Poisson(lambda): inversion below 12, PTRS transformed rejection above
  * (W. Hoermann, "The transformed rejection method for generating Poisson
- * random variables", Insurance: Mathematics and Economics 12, 1993). */
-PCS_HD uint32_t pcs_poisson(double lam, uint32_t video, uint32_t slot, uint32_t gt, uint32_t k0, uint32_t k1)
+ * random variables", Insurance: Mathematics and Economics 12, 1993).  The
+ * constants depend on lambda only, so a proposal computes them once for all
+ * of its videos. */
+struct PoissonSetup {
+    double lam, explam, loglam, b, a, invalpha, vr, log_invalpha;
+};
+
+PCS_HD PoissonSetup pcs_poisson_setup(double lam)
 {
+    PoissonSetup ps;
+    ps.lam = lam;
+    ps.explam = ps.loglam = ps.b = ps.a = ps.invalpha = ps.vr = ps.log_invalpha = 0.0;
+    if (!(lam > 0.0)) return ps;
+    if (lam < 12.0) {
+        ps.explam = exp(-lam);
+        return ps;
+    }
+    const double slam = sqrt(lam);
+    ps.loglam = log(lam);
+    ps.b = 0.931 + 2.53 * slam;
+    ps.a = -0.059 + 0.02483 * ps.b;
+    ps.invalpha = 1.1239 + 1.1328 / (ps.b - 3.4);
+    ps.vr = 0.9277 - 3.6224 / (ps.b - 2.0);
+    ps.log_invalpha = log(ps.invalpha);
+    return ps;
+}
+
+PCS_HD uint32_t pcs_poisson_draw(const PoissonSetup& ps, uint32_t video, uint32_t slot, uint32_t gt, uint32_t k0,
+                                 uint32_t k1)
+{
+    const double lam = ps.lam;
     if (!(lam > 0.0)) return 0u;
     if (lam < 12.0) {
         const pcs_u4 r = pcs_draw(video, pcs_ctr_tag(PCS_STREAM_POISSON, 0u), slot, gt, k0, k1);
         const double u = pcs_u01_53(r.x, r.y);
-        double p = exp(-lam), F = p;
+        double p = ps.explam, F = p;
         uint32_t k = 0;
         while (u > F && k < 1000u) {
             ++k;
@@ -88,23 +116,24 @@ PCS_HD uint32_t pcs_poisson(double lam, uint32_t video, uint32_t slot, uint32_t 
         }
         return k;
     }
-    const double slam = sqrt(lam), loglam = log(lam);
-    const double b = 0.931 + 2.53 * slam;
-    const double a = -0.059 + 0.02483 * b;
-    const double invalpha = 1.1239 + 1.1328 / (b - 3.4);
-    const double vr = 0.9277 - 3.6224 / (b - 2.0);
+    const double a = ps.a, b = ps.b;
     for (uint32_t it = 0; it < 256u; ++it) {
         const pcs_u4 r = pcs_draw(video, pcs_ctr_tag(PCS_STREAM_POISSON, 1u + it), slot, gt, k0, k1);
         const double U = pcs_u01_53(r.x, r.y) - 0.5;
         const double V = pcs_u01_53(r.z, r.w);
         const double us = 0.5 - fabs(U);
         const double kf = floor((2.0 * a / us + b) * U + lam + 0.43);
-        if (us >= 0.07 && V <= vr) return (uint32_t)kf;
+        if (us >= 0.07 && V <= ps.vr) return (uint32_t)kf;
         if (kf < 0.0 || (us < 0.013 && V > us)) continue;
-        if (log(V) + log(invalpha) - log(a / (us * us) + b) <= -lam + kf * loglam - lgamma(kf + 1.0))
+        if (log(V) + ps.log_invalpha - log(a / (us * us) + b) <= -lam + kf * ps.loglam - lgamma(kf + 1.0))
             return (uint32_t)kf;
     }
     return (uint32_t)floor(lam + 0.5);
+}
+
+PCS_HD uint32_t pcs_poisson(double lam, uint32_t video, uint32_t slot, uint32_t gt, uint32_t k0, uint32_t k1)
+{
+    return pcs_poisson_draw(pcs_poisson_setup(lam), video, slot, gt, k0, k1);
 }
 
 /* first cumulative weight >= u (std::lower_bound), clamped to N - 1 */
@@ -121,46 +150,29 @@ PCS_HD uint32_t pcs_pick(const double* wcum, uint32_t N, double u)
     return lo < N ? lo : N - 1;
 }
 
-/* Parameters of trial `trial` of population slot `slot` in generation `gen`.
- * Generation 0 (the prior pass) simulates the slot's own parameters. */
-PCS_HD void pcs_build_theta(const JobPmcDev& pm, const double* theta_pop, const double* wcum,
-                            const double* factor, uint32_t slot, uint32_t trial, uint32_t gen,
-                            uint32_t k0, uint32_t k1, double* th)
+/* Parameter p of a perturbed proposal: parent value tp[p] displaced by the
+ * perturbation factor applied to the normals nrm[0..p] (Cholesky) or nrm[p]
+ * (diagonal), reflected into the prior box; fixed parameters stay at lo. */
+PCS_HD double pcs_perturb_one(const JobPmcDev& pm, const double* tp, const double* factor, const double* nrm,
+                              uint32_t p)
 {
-    const uint32_t P = pm.P, N = pm.N;
+    const uint32_t P = pm.P;
+    if (pm.fixed[p]) return pm.lo[p];
+    double delta;
+    if (pm.perturbation == 1u) {
+        delta = 0.0;
+        for (uint32_t i = 0; i <= p; ++i)
+            if (!pm.fixed[i]) delta += factor[p * P + i] * nrm[i];
+    } else {
+        delta = factor[p * P + p] * nrm[p];
+    }
+    return pcs_reflect(tp[p] + delta, pm.lo[p], pm.hi[p]);
+}
+
+/* Sort the components by the first parameter group (label switching). */
+PCS_HD void pcs_sort_components(const JobPmcDev& pm, double* th)
+{
     const Layout L = pcs_layout(pm);
-    const uint32_t gt = pcs_ctr_gen_trial(gen, trial);
-    if (gen == 0u) {
-        for (uint32_t p = 0; p < P; ++p) th[p] = theta_pop[(uint64_t)slot * P + p];
-        return;
-    }
-    const pcs_u4 r = pcs_draw(0u, pcs_ctr_tag(PCS_STREAM_PICK, 0u), slot, gt, k0, k1);
-    const uint32_t parent = pcs_pick(wcum, N, pcs_u01_53(r.x, r.y));
-    const double* tp = theta_pop + (uint64_t)parent * P;
-    double nrm[PCS_MAX_P];
-    for (uint32_t p = 0; p < P; p += 2) {
-        const pcs_u4 rr = pcs_draw(p >> 1, pcs_ctr_tag(PCS_STREAM_PERTURB, 0u), slot, gt, k0, k1);
-        double n0, n1;
-        pcs_normal2(rr, n0, n1);
-        nrm[p] = n0;
-        if (p + 1 < P) nrm[p + 1] = n1;
-    }
-    for (uint32_t p = 0; p < P; ++p) {
-        if (pm.fixed[p]) {
-            th[p] = pm.lo[p];
-            continue;
-        }
-        double delta;
-        if (pm.perturbation == 1u) {
-            delta = 0.0;
-            for (uint32_t i = 0; i <= p; ++i)
-                if (!pm.fixed[i]) delta += factor[p * P + i] * nrm[i];
-        } else {
-            delta = factor[p * P + p] * nrm[p];
-        }
-        th[p] = pcs_reflect(tp[p] + delta, pm.lo[p], pm.hi[p]);
-    }
-    /* sort components by the first parameter group (label switching) */
     for (uint32_t i = 1; i < L.C; ++i) {
         for (uint32_t x = i; x > 0 && th[L.m + x] < th[L.m + x - 1]; --x) {
             double t;
@@ -184,15 +196,66 @@ PCS_HD void pcs_build_theta(const JobPmcDev& pm, const double* theta_pop, const 
     }
 }
 
-/* Forward-model arguments of a proposal; returns the Poisson mean per video. */
-PCS_HD double pcs_build_args(const JobPmcDev& pm, const double* th, uint32_t gen, PropDev& pd)
+/* Parameters of trial `trial` of population slot `slot` in generation `gen`.
+ * Generation 0 (the prior pass) simulates the slot's own parameters. */
+PCS_HD void pcs_build_theta(const JobPmcDev& pm, const double* theta_pop, const double* wcum,
+                            const double* factor, uint32_t slot, uint32_t trial, uint32_t gen,
+                            uint32_t k0, uint32_t k1, double* th)
+{
+    const uint32_t P = pm.P, N = pm.N;
+    const uint32_t gt = pcs_ctr_gen_trial(gen, trial);
+    if (gen == 0u) {
+        for (uint32_t p = 0; p < P; ++p) th[p] = theta_pop[(uint64_t)slot * P + p];
+        return;
+    }
+    const pcs_u4 r = pcs_draw(0u, pcs_ctr_tag(PCS_STREAM_PICK, 0u), slot, gt, k0, k1);
+    const uint32_t parent = pcs_pick(wcum, N, pcs_u01_53(r.x, r.y));
+    const double* tp = theta_pop + (uint64_t)parent * P;
+    double nrm[PCS_MAX_P];
+    for (uint32_t p = 0; p < P; p += 2) {
+        const pcs_u4 rr = pcs_draw(p >> 1, pcs_ctr_tag(PCS_STREAM_PERTURB, 0u), slot, gt, k0, k1);
+        double n0, n1;
+        pcs_normal2(rr, n0, n1);
+        nrm[p] = n0;
+        if (p + 1 < P) nrm[p + 1] = n1;
+    }
+    for (uint32_t p = 0; p < P; ++p) th[p] = pcs_perturb_one(pm, tp, factor, nrm, p);
+    pcs_sort_components(pm, th);
+}
+
+/* Per-component forward-model arguments: 10^log10c and the step sd's scale
+ * and shape (lognormal) or the fixed step sd. */
+struct CompArgs {
+    double powc;
+    float sd_scale, sd_shape;
+};
+
+PCS_HD CompArgs pcs_comp_args(const JobPmcDev& pm, const double* th, uint32_t i)
 {
     const Layout L = pcs_layout(pm);
-    double powc[PCS_MAX_C], csum = 0.0;
-    for (uint32_t i = 0; i < L.C; ++i) {
-        powc[i] = pow(10.0, th[L.c + i]);
-        csum += powc[i];
+    CompArgs ca;
+    ca.powc = pow(10.0, th[L.c + i]);
+    if (pm.model == PCS_DEV_MODEL_LOGNORMAL) {
+        /* lognormal diameter (nm), mean mu and sd s: sigma_ln^2 = ln(1 + s^2 / mu^2) */
+        const double mu = th[L.m + i], sdv = th[L.s + i];
+        const double sl2 = log1p((sdv * sdv) / (mu * mu));
+        const double mul = log(mu) - 0.5 * sl2;
+        ca.sd_scale = (float)(pm.sd_const * exp(-0.5 * mul));
+        ca.sd_shape = (float)(-0.5 * sqrt(sl2));
+    } else {
+        ca.sd_scale = (float)sqrt(2.0 * th[L.m + i] * pm.delta_t);
+        ca.sd_shape = 0.0f;
     }
+    return ca;
+}
+
+/* Assembles a proposal's forward-model arguments from its components';
+ * returns the Poisson mean per video. */
+PCS_HD double pcs_assemble_args(const JobPmcDev& pm, const double* th, const CompArgs* ca, uint32_t gen, PropDev& pd)
+{
+    const Layout L = pcs_layout(pm);
+    double csum = 0.0;
+    for (uint32_t i = 0; i < L.C; ++i) csum += ca[i].powc;
     for (uint32_t i = 0; i < PCS_MAX_C; ++i) {
         pd.pre_comp_prob[i] = 2.0f;
         pd.sd_scale[i] = 0.0f;
@@ -201,18 +264,10 @@ PCS_HD double pcs_build_args(const JobPmcDev& pm, const double* th, uint32_t gen
     }
     double acc = 0.0;
     for (uint32_t i = 0; i < L.C; ++i) {
-        acc += powc[i] / csum;
+        acc += ca[i].powc / csum;
         pd.pre_comp_prob[i] = (float)acc;
-        if (pm.model == PCS_DEV_MODEL_LOGNORMAL) {
-            /* lognormal diameter (nm), mean mu and sd s: sigma_ln^2 = ln(1 + s^2 / mu^2) */
-            const double mu = th[L.m + i], sdv = th[L.s + i];
-            const double sl2 = log1p((sdv * sdv) / (mu * mu));
-            const double mul = log(mu) - 0.5 * sl2;
-            pd.sd_scale[i] = (float)(pm.sd_const * exp(-0.5 * mul));
-            pd.sd_shape[i] = (float)(-0.5 * sqrt(sl2));
-        } else {
-            pd.sd_scale[i] = (float)sqrt(2.0 * th[L.m + i] * pm.delta_t);
-        }
+        pd.sd_scale[i] = ca[i].sd_scale;
+        pd.sd_shape[i] = ca[i].sd_shape;
     }
     pd.pre_comp_prob[L.C - 1] = 2.0f;
     for (uint32_t z = 0; z < L.Z; ++z) {
@@ -222,6 +277,14 @@ PCS_HD double pcs_build_args(const JobPmcDev& pm, const double* th, uint32_t gen
     return csum * pm.volume_factor;
 }
 
+/* Forward-model arguments of a proposal; returns the Poisson mean per video. */
+PCS_HD double pcs_build_args(const JobPmcDev& pm, const double* th, uint32_t gen, PropDev& pd)
+{
+    CompArgs ca[PCS_MAX_C];
+    for (uint32_t i = 0; i < pm.C; ++i) ca[i] = pcs_comp_args(pm, th, i);
+    return pcs_assemble_args(pm, th, ca, gen, pd);
+}
+
 /* Poisson counts per video and their prefix; returns total particles (and
  * particle-steps through *steps). */
 PCS_HD uint64_t pcs_draw_counts(double lambda, uint32_t V, const uint32_t* frames, uint32_t slot,
@@ -229,10 +292,11 @@ PCS_HD uint64_t pcs_draw_counts(double lambda, uint32_t V, const uint32_t* frame
                                 uint32_t* pre, uint64_t* steps)
 {
     const uint32_t gt = pcs_ctr_gen_trial(gen, trial);
+    const PoissonSetup ps = pcs_poisson_setup(lambda);
     uint64_t total = 0, st = 0;
     pre[0] = 0u;
     for (uint32_t v = 0; v < V; ++v) {
-        const uint32_t c = pcs_poisson(lambda, v, slot, gt, k0, k1);
+        const uint32_t c = pcs_poisson_draw(ps, v, slot, gt, k0, k1);
         cnt[v] = c;
         total += c;
         st += (uint64_t)c * frames[v];
