@@ -478,6 +478,10 @@ def main():
     dist_ms = ks.distance_ms / max(1, ks.distance_launches)
     dist_gbs = (ks.histogram_cells / max(1, ks.distance_launches)) * DIST_BYTES_PER_CELL / (dist_ms / 1e3) / 1e9
 
+    pmc_s = max(ks.pmc_ms, 1e-9) / 1e3
+    pmc_gbs = ks.pmc_bytes / pmc_s / 1e9
+    pmc_tflops = ks.pmc_pair_flops / pmc_s / 1e12
+
     cells = ks.histogram_cells / max(1, ks.rounds)
     l2_note = (f"round histograms {cells * 4 / 1e6:.0f} MB per round + job state"
                + (" (above L2)" if cells * 4 > 129e6 else " (below L2; the kernels are issue-bound)"))
@@ -504,6 +508,13 @@ def main():
         "roofline_distance": {"bound": "hbm", "achieved": dist_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                               "frac": dist_gbs / float(peaks.get("hbm_gbs", 6800.0)),
                               "kernel": "k_distance", "peak_src": peak_src},
+        "roofline_pmc": {"bound": "hbm", "achieved": pmc_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": pmc_gbs / float(peaks.get("hbm_gbs", 6800.0)),
+                         "kernel": "k_accept + k_whiten + k_kernel_sum + k_finalize (the PMC step)",
+                         "achieved_def": "(2 N P x 8 population read + write + N x 8 weights) per ended generation / "
+                                         "PMC-step time of all rounds",
+                         "pair_tflops": pmc_tflops, "generations": int(ks.generations),
+                         "ms_per_generation": ks.pmc_ms / max(1, ks.generations), "peak_src": peak_src},
         "kernel_ms": {"simulate_per_launch": sim_ms, "distance_per_launch": dist_ms,
                       "rounds": int(ks.rounds), "round_ms_total": ks.round_ms},
         "clocks": clk,

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define PCS_ABI_VERSION 2
+#define PCS_ABI_VERSION 3
 #define PCS_MAX_COMPONENTS 8
 
 typedef enum pcs_status {
@@ -190,6 +190,14 @@ typedef struct pcs_kernel_stats {
     uint64_t particle_steps;      /* walk steps incl. initial placements */
     uint64_t histogram_cells;     /* R x B cells scanned by the distance kernel */
     uint64_t split_tasks;         /* slab-split walk: groups of four steps walked in x, y */
+    /* the PMC step: accept, whiten, pairwise kernel sum, finalize (one timed
+     * span per round; they do their generation-end work only in rounds that
+     * end a job's generation) */
+    uint64_t pmc_launches;        /* rounds whose PMC-step span was timed */
+    double pmc_ms;                /* sum of the spans */
+    uint64_t generations;         /* generations ended across jobs (prior pass included) */
+    uint64_t pmc_bytes;           /* per ended generation: population read + write 2 x N x P x 8, weights N x 8 */
+    uint64_t pmc_pair_flops;      /* pmc-standard kernel sum: N^2 x (6P + 7) per committed generation > 0 */
 } pcs_kernel_stats;
 pcs_status pcs_get_kernel_stats(pcs_ctx* ctx, pcs_kernel_stats* out);
 pcs_status pcs_reset_kernel_stats(pcs_ctx* ctx);

@@ -80,7 +80,9 @@ class KernelStats(C.Structure):
         ("rounds", C.c_uint64), ("kernel_launches", C.c_uint64), ("simulate_launches", C.c_uint64),
         ("simulate_ms", C.c_double), ("distance_launches", C.c_uint64), ("distance_ms", C.c_double),
         ("round_ms", C.c_double), ("proposals", C.c_uint64), ("particle_steps", C.c_uint64),
-        ("histogram_cells", C.c_uint64), ("split_tasks", C.c_uint64),
+        ("histogram_cells", C.c_uint64), ("split_tasks", C.c_uint64), ("pmc_launches", C.c_uint64),
+        ("pmc_ms", C.c_double), ("generations", C.c_uint64), ("pmc_bytes", C.c_uint64),
+        ("pmc_pair_flops", C.c_uint64),
     ]
 
 

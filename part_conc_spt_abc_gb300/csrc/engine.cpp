@@ -415,7 +415,7 @@ Ctx::Ctx(int dev, int infl) : device(dev), inflight(infl > 0 ? infl : 1)
     *h_err = 0;
     PCS_CUDA(cudaEventCreate(&ev0));
     PCS_CUDA(cudaEventCreate(&ev1));
-    for (cudaEvent_t* e : {&ev_sim0, &ev_sim1, &ev_dist0, &ev_dist1, &ev_t0, &ev_t1}) PCS_CUDA(cudaEventCreate(e));
+    for (cudaEvent_t* e : {&ev_sim0, &ev_sim1, &ev_dist0, &ev_dist1, &ev_pmc0, &ev_pmc1, &ev_t0, &ev_t1}) PCS_CUDA(cudaEventCreate(e));
     PCS_CUDA(cudaMallocHost((void**)&h_round_out, sizeof(RoundDev)));
     std::memset(h_round_out, 0, sizeof(RoundDev));
 }
@@ -430,7 +430,7 @@ Ctx::~Ctx()
     if (h_round) cudaFreeHost(h_round);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
-    for (cudaEvent_t e : {ev_sim0, ev_sim1, ev_dist0, ev_dist1, ev_t0, ev_t1})
+    for (cudaEvent_t e : {ev_sim0, ev_sim1, ev_dist0, ev_dist1, ev_pmc0, ev_pmc1, ev_t0, ev_t1})
         if (e) cudaEventDestroy(e);
     if (h_round_out) cudaFreeHost(h_round_out);
     if (stream) cudaStreamDestroy(stream);
@@ -592,8 +592,10 @@ void Ctx::enqueue_round()
     PCS_CUDA(launch_distance(d, std::min<uint32_t>(rb.capacity, (uint32_t)(distance_ctas_per_sm(rb.max_rows) * sm_count)), stream));
     PCS_CUDA(cudaEventRecordWithFlags(ev_dist1, stream, cudaEventRecordExternal));
 
+    PCS_CUDA(cudaEventRecordWithFlags(ev_pmc0, stream, cudaEventRecordExternal));
     PCS_CUDA(launch_accept(a, kMaxRoundJobs, stream));
     PCS_CUDA(launch_finalize(a, kMaxRoundJobs, rb.max_n, stream));
+    PCS_CUDA(cudaEventRecordWithFlags(ev_pmc1, stream, cudaEventRecordExternal));
     PCS_CUDA(cudaMemcpyAsync(h_status, rb.pmc.p, sizeof(JobPmcDev) * kMaxRoundJobs, cudaMemcpyDeviceToHost, stream));
     PCS_CUDA(cudaMemcpyAsync(h_err, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
     PCS_CUDA(cudaMemcpyAsync(h_round_out, rb.round.p, sizeof(RoundDev), cudaMemcpyDeviceToHost, stream));
@@ -629,10 +631,11 @@ void Ctx::run_round(double* ms_out)
     }
     PCS_CUDA(cudaEventRecord(ev1, stream));
     PCS_CUDA(cudaStreamSynchronize(stream));
-    float ms = 0.0f, sim_ms = 0.0f, dist_ms = 0.0f;
+    float ms = 0.0f, sim_ms = 0.0f, dist_ms = 0.0f, pmc_ms = 0.0f;
     PCS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
     PCS_CUDA(cudaEventElapsedTime(&sim_ms, ev_sim0, ev_sim1));
     PCS_CUDA(cudaEventElapsedTime(&dist_ms, ev_dist0, ev_dist1));
+    PCS_CUDA(cudaEventElapsedTime(&pmc_ms, ev_pmc0, ev_pmc1));
     if (ms_out) *ms_out = ms;
     stats.rounds += 1;
     stats.kernel_launches += kKernelsPerRound;
@@ -641,6 +644,8 @@ void Ctx::run_round(double* ms_out)
     stats.distance_launches += 1;
     stats.distance_ms += dist_ms;
     stats.round_ms += ms;
+    stats.pmc_launches += 1;
+    stats.pmc_ms += pmc_ms;
     stats.proposals += h_round_out->n_props;
     stats.particle_steps += h_round_out->round_steps;
     stats.histogram_cells += h_round_out->round_cells;
@@ -654,7 +659,17 @@ void Ctx::run_round(double* ms_out)
     }
     for (size_t i = 0; i < table.size(); ++i)
         if (table[i]) {
-            table[i]->status = h_status[i];
+            const JobPmcDev& was = table[i]->status;
+            const JobPmcDev& now = h_status[i];
+            if (now.iterations > was.iterations) {
+                /* this round ended generation `was.generation` of the job */
+                const uint64_t N = now.N, P = now.P;
+                stats.generations += 1;
+                stats.pmc_bytes += 2ull * N * P * 8ull + N * 8ull;
+                if (was.generation > 0u && now.weighting == 0u && !now.converged)
+                    stats.pmc_pair_flops += N * N * (6ull * P + 7ull);
+            }
+            table[i]->status = now;
             table[i]->device_ms += ms;
         }
 }

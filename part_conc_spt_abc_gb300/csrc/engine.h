@@ -95,6 +95,7 @@ struct Ctx {
     uint64_t mem_used = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t ev_sim0 = nullptr, ev_sim1 = nullptr, ev_dist0 = nullptr, ev_dist1 = nullptr;
+    cudaEvent_t ev_pmc0 = nullptr, ev_pmc1 = nullptr;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
     RoundDev* h_round_out = nullptr; /* pinned copy of the round counters */
     pcs_kernel_stats stats{};

@@ -238,3 +238,31 @@ def test_autotune(pcs, ctx):
     t = ctx.autotune(inp)
     assert t.block_size in (128, 256, 512, 1024) and t.particles_per_thread in (1, 2, 4)
     ctx.set_tuning(block_size=256, particles_per_thread=1, hist_tile_rows=64, warp_aggregate=0xFFFFFFFF)
+
+
+def test_kernel_stats_account_for_the_rounds(pcs, ctx):
+    """The per-kernel accounting that the benchmark's rooflines divide by:
+    every round is counted with its launches and timed spans, steps and
+    proposals match the job's own counters, and each ended generation adds
+    its population bytes (and, after the prior pass, its pairwise kernel-sum
+    FLOPs under pmc-standard weights)."""
+    inp, _ = small_input(pcs, C=2)
+    p = inp.params
+    ctx.reset_kernel_stats()
+    sim = pcs.make_simulation(ctx, inp, 11)
+    for _ in range(3):
+        sim.step()
+    info = sim.info()
+    sim.close()
+    ks = ctx.kernel_stats()
+    N, P = p.abc_sample_count, info.param_count
+    assert ks.rounds > 0
+    assert ks.kernel_launches == 9 * ks.rounds
+    assert ks.simulate_launches == ks.rounds == ks.distance_launches == ks.pmc_launches
+    assert ks.simulate_ms > 0 and ks.distance_ms > 0 and ks.pmc_ms > 0
+    assert ks.simulate_ms + ks.distance_ms + ks.pmc_ms <= ks.round_ms * (1 + 1e-6)
+    assert ks.particle_steps == info.particle_steps
+    assert ks.proposals == info.simulations
+    assert ks.generations == 3  # the prior pass and two generations
+    assert ks.pmc_bytes == 3 * (2 * N * P * 8 + N * 8)
+    assert ks.pmc_pair_flops == 2 * N * N * (6 * P + 7)
