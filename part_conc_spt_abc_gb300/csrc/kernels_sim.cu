@@ -104,11 +104,14 @@ __device__ __forceinline__ void record_(const ItemCtx& c, uint32_t* tile, uint32
     record_out_<AGG>(c.four_dt, c.dde, c.B, c.RB, c.tile_rows, c.hist, c.err, tile, k, de);
 }
 
-template <bool AGG>
+/* One frame of the walk.  CHECK: the frame may lie past the particle's
+ * last one (s >= F) and is then skipped; full groups of four frames call it
+ * without the test. */
+template <bool AGG, bool CHECK = true>
 __device__ __forceinline__ void step_(const ItemCtx& c, uint32_t* tile, Walker& w, uint32_t s,
                                       float n0, float n1, float n2)
 {
-    if (s >= w.F) return;
+    if (CHECK && s >= w.F) return;
     float dx = __fmul_rn(w.sd, n0);
     w.x = wrap_(__fadd_rn(w.x, dx), c.hlx, c.two_hlx);
     float dy = __fmul_rn(w.sd, n1);
@@ -242,6 +245,27 @@ __device__ __forceinline__ void init_walker_(const SimArgs& a, const ItemCtx& c,
     q.k = det ? 1u : 0u;
 }
 
+/* The 12 normals of the group of frames s0 .. s0+3: Philox blocks
+ * 2+3g .. 4+3g through Box-Muller, or the replayed normals (zeros past F). */
+template <bool REPLAY>
+__device__ __forceinline__ void group_normals_(const SimArgs& a, const Walker& q, uint32_t s0, float* nn)
+{
+    if (REPLAY) {
+        const float* src = a.rp_normals + ((uint64_t)q.n * a.rp_stride + (s0 - 1u)) * 3u;
+        const uint32_t rem = min(4u, q.F - s0);
+#pragma unroll
+        for (int t = 0; t < 12; ++t) nn[t] = ((uint32_t)t < rem * 3u) ? src[t] : 0.0f;
+    } else {
+        const uint32_t g = (s0 - 1u) >> 2;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 2u + 3u * g + (uint32_t)b));
+            box_muller_(r.x, r.y, nn[4 * b + 0], nn[4 * b + 1]);
+            box_muller_(r.z, r.w, nn[4 * b + 2], nn[4 * b + 3]);
+        }
+    }
+}
+
 } // namespace
 
 template <int PPT, bool REPLAY, bool AGG>
@@ -295,27 +319,35 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
                 }
             }
 
-            /* frames 1 .. F-1, four per group */
+            /* frames 1 .. F-1, four per group; one walker per thread: the
+             * full groups skip the per-frame end test, the tail group keeps it */
+            if (PPT == 1) {
+                Walker& q = w[0];
+                uint32_t s0 = 1;
+                for (; s0 + 3u < q.F; s0 += 4u) {
+                    float nn[12];
+                    group_normals_<REPLAY>(a, q, s0, nn);
+                    step_<AGG, false>(c, s_tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
+                    step_<AGG, false>(c, s_tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
+                    step_<AGG, false>(c, s_tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
+                    step_<AGG, false>(c, s_tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
+                }
+                if (s0 < q.F) {
+                    float nn[12];
+                    group_normals_<REPLAY>(a, q, s0, nn);
+                    step_<AGG>(c, s_tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
+                    step_<AGG>(c, s_tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
+                    step_<AGG>(c, s_tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
+                    step_<AGG>(c, s_tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
+                }
+            } else
             for (uint32_t s0 = 1; s0 < fmax; s0 += 4u) {
-                const uint32_t g = (s0 - 1u) >> 2;
 #pragma unroll
                 for (int j = 0; j < PPT; ++j) {
                     Walker& q = w[j];
                     if (s0 >= q.F) continue;
                     float nn[12];
-                    if (REPLAY) {
-                        const float* src = a.rp_normals + ((uint64_t)q.n * a.rp_stride + (s0 - 1u)) * 3u;
-                        const uint32_t rem = min(4u, q.F - s0);
-#pragma unroll
-                        for (int t = 0; t < 12; ++t) nn[t] = ((uint32_t)t < rem * 3u) ? src[t] : 0.0f;
-                    } else {
-#pragma unroll
-                        for (int b = 0; b < 3; ++b) {
-                            pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 2u + 3u * g + (uint32_t)b));
-                            box_muller_(r.x, r.y, nn[4 * b + 0], nn[4 * b + 1]);
-                            box_muller_(r.z, r.w, nn[4 * b + 2], nn[4 * b + 3]);
-                        }
-                    }
+                    group_normals_<REPLAY>(a, q, s0, nn);
                     step_<AGG>(c, s_tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
                     step_<AGG>(c, s_tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
                     step_<AGG>(c, s_tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
