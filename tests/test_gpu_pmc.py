@@ -10,14 +10,14 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def small_input(pcs, seed=0, C=1, schedule=None, weighting=0, model=None, videos=6, frames=60, pop=96):
+def small_input(pcs, seed=0, C=1, schedule=None, weighting=0, model=None, videos=6, frames=60, pop=96, de_bins=48):
     import part_conc_spt_abc_gb300.workloads as W
     ctx = pcs.Context(0)
     try:
         mu = [175.0, 500.0][:C]
         sd = [10.0, 25.0][:C]
         w = [0.6, 0.4][:C]
-        inp, truth = W.make_problem(ctx, mu, sd, 3e14, w, videos, frames, 48, pop, 4, seed=seed)
+        inp, truth = W.make_problem(ctx, mu, sd, 3e14, w, videos, frames, de_bins, pop, 4, seed=seed)
     finally:
         ctx.close()
     p = inp.params
@@ -139,6 +139,30 @@ def test_serve_alone_equals_mix(pcs, ctx):
                 assert np.array_equal(getattr(a, f), getattr(b, f)), (order, f)
             s.close()
     ctx.set_tuning(job_order=2, round_capacity=2048)
+
+
+def test_serve_mixed_shapes_alone_equals_mix(pcs, ctx):
+    """Jobs whose histograms differ in rows and bins (61 x 48, 91 x 37,
+    46 x 64, 121 x 130) share the rounds: the distance kernel then moves from
+    one proposal's shape to another's inside a launch, and every job's result
+    is still the one it gets alone."""
+    shapes = [(60, 48), (90, 37), (45, 64), (120, 130)]
+    jobs = [small_input(pcs, seed=10 + i, C=1 + i % 2, pop=48, frames=f, de_bins=b)[0]
+            for i, (f, b) in enumerate(shapes)]
+    alone = [run_job(pcs, ctx, inp, 200 + i, 1000)[0] for i, inp in enumerate(jobs)]
+    srv = pcs.Server(ctx)
+    sims = [pcs.make_simulation(ctx, inp, 200 + i) for i, inp in enumerate(jobs)]
+    for s in sims:
+        srv.submit(s)
+    for _ in range(100000):
+        if srv.step() == 0:
+            break
+    for s, a in zip(sims, alone):
+        assert srv.finished(s)
+        b = s.output()
+        for f in ["m", "c", "az", "dist", "w"]:
+            assert np.array_equal(getattr(a, f), getattr(b, f)), f
+        s.close()
 
 
 def test_serve_memory_cap(pcs, ctx):
