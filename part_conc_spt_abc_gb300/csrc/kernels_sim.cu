@@ -266,6 +266,70 @@ __device__ __forceinline__ void group_normals_(const SimArgs& a, const Walker& q
     }
 }
 
+/* Frames 1 .. F-1 of one walker, four per group: the full groups skip the
+ * per-frame end test, the tail group keeps it. */
+template <bool REPLAY, bool AGG>
+__device__ __forceinline__ void walk_single_(const SimArgs& a, const ItemCtx& c, uint32_t* tile, Walker& q)
+{
+    uint32_t s0 = 1;
+    for (; s0 + 3u < q.F; s0 += 4u) {
+        float nn[12];
+        group_normals_<REPLAY>(a, q, s0, nn);
+        step_<AGG, false>(c, tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
+        step_<AGG, false>(c, tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
+        step_<AGG, false>(c, tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
+        step_<AGG, false>(c, tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
+    }
+    if (s0 < q.F) {
+        float nn[12];
+        group_normals_<REPLAY>(a, q, s0, nn);
+        step_<AGG>(c, tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
+        step_<AGG>(c, tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
+        step_<AGG>(c, tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
+        step_<AGG>(c, tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
+    }
+}
+
+/* Work without a shared-memory histogram tile (every record a global
+ * atomic): nothing ties a CTA's warps to one work item, so each warp takes
+ * its own 32-particle slice of an item from the queue (slice s is part
+ * s % slices of item s / slices) and no CTA barrier is needed.  Same walkers,
+ * same draws, same records as the CTA loop. */
+template <bool AGG>
+__device__ __noinline__ void simulate_warp_slices_(const SimArgs& a)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t slices = (a.chunk + 31u) / 32u;
+    const uint32_t n_slices = *a.n_items * slices;
+    for (;;) {
+        uint32_t sl = 0u;
+        if (lane == 0u) sl = atomicAdd(a.queue_head, 1u);
+        sl = __shfl_sync(0xFFFFFFFFu, sl, 0);
+        if (sl >= n_slices) break;
+        const uint32_t item = sl / slices, part = sl - item * slices;
+        const PropDev& prop = a.props[a.item_prop[item]];
+        const JobDev& job = a.jobs[prop.job];
+        const ItemCtx c = item_ctx_(a, job, prop);
+        const uint32_t i0 = (item - prop.item_begin) * a.chunk;
+        const uint32_t i1 = min(i0 + a.chunk, prop.total_particles);
+        const uint32_t n = i0 + part * 32u + lane;
+        if (n < i1) {
+            Walker q;
+            q.n = n;
+            q.F = 0;
+            q.k = 0;
+            q.de = 0.0f;
+            q.x = q.y = q.z = 0.0f;
+            q.sd = 0.0f;
+            q.haz = 0.0f;
+            init_walker_<false>(a, c, job, prop, a.counts + prop.counts_off + job.V, n, prop.slot,
+                                pcs_ctr_gen_trial(prop.gen, prop.trial), job.seed_lo, job.seed_hi, q);
+            walk_single_<false, AGG>(a, c, nullptr, q);
+            if (q.F > 0u && q.k >= c.kmin) record_<AGG>(c, nullptr, q.k, q.de);
+        }
+    }
+}
+
 } // namespace
 
 template <int PPT, bool REPLAY, bool AGG>
@@ -276,6 +340,10 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
     __shared__ PropDev s_prop;
     __shared__ JobDev s_job;
 
+    if (!REPLAY && PPT == 1 && a.tile_words == 0u) {
+        simulate_warp_slices_<AGG>(a);
+        return;
+    }
     const uint32_t tid = threadIdx.x, bd = blockDim.x;
     for (uint32_t i = tid; i < a.tile_words; i += bd) s_tile[i] = 0u;
     const uint32_t n_items = *a.n_items;
@@ -322,24 +390,7 @@ __global__ void __launch_bounds__(1024) k_simulate(SimArgs a)
             /* frames 1 .. F-1, four per group; one walker per thread: the
              * full groups skip the per-frame end test, the tail group keeps it */
             if (PPT == 1) {
-                Walker& q = w[0];
-                uint32_t s0 = 1;
-                for (; s0 + 3u < q.F; s0 += 4u) {
-                    float nn[12];
-                    group_normals_<REPLAY>(a, q, s0, nn);
-                    step_<AGG, false>(c, s_tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
-                    step_<AGG, false>(c, s_tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
-                    step_<AGG, false>(c, s_tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
-                    step_<AGG, false>(c, s_tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
-                }
-                if (s0 < q.F) {
-                    float nn[12];
-                    group_normals_<REPLAY>(a, q, s0, nn);
-                    step_<AGG>(c, s_tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
-                    step_<AGG>(c, s_tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
-                    step_<AGG>(c, s_tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
-                    step_<AGG>(c, s_tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
-                }
+                walk_single_<REPLAY, AGG>(a, c, s_tile, w[0]);
             } else
             for (uint32_t s0 = 1; s0 < fmax; s0 += 4u) {
 #pragma unroll

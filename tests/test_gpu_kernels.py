@@ -208,7 +208,9 @@ def test_philox_determinism_and_independence(pcs, ctx, oracle, walk):
     assert not np.array_equal(b[0], c[0])
     # independent of the launch shape
     for kw in [dict(block_size=128, particles_per_thread=1), dict(block_size=512, particles_per_thread=2),
-               dict(block_size=256, particles_per_thread=4, warp_aggregate=1)]:
+               dict(block_size=256, particles_per_thread=4, warp_aggregate=1),
+               dict(block_size=256, particles_per_thread=1, hist_tile_rows=0xFFFFFFFF),  # warp slices
+               dict(block_size=1024, particles_per_thread=1, hist_tile_rows=0xFFFFFFFF, warp_aggregate=1)]:
         ctx.set_tuning(**kw)
         d = pcs.simulate_hist(ctx, setup, [run], seed=7)
         assert np.array_equal(d[0], b[0]), kw

@@ -73,7 +73,10 @@ def test_results_do_not_depend_on_batching(pcs, ctx, walk):
                 dict(round_capacity=200, max_speculation=64),
                 dict(max_speculation=4096, block_size=512, particles_per_thread=4, hist_tile_rows=8,
                      warp_aggregate=1),
-                dict(round_fill=0xFFFFFFFF), dict(round_fill=3000000), dict(job_order=2)]
+                dict(round_fill=0xFFFFFFFF), dict(round_fill=3000000), dict(job_order=2),
+                # no shared-memory tile: each warp takes its own slices of the work items
+                dict(hist_tile_rows=0xFFFFFFFF, block_size=256, particles_per_thread=1, warp_aggregate=0xFFFFFFFF),
+                dict(hist_tile_rows=0xFFFFFFFF, block_size=1024, particles_per_thread=1, warp_aggregate=1)]
     try:
         for kw in settings:
             ctx.set_tuning(**kw)
