@@ -139,7 +139,9 @@ size_t pcs_device_report(char* buf, size_t cap);
 typedef struct pcs_tuning {
     uint32_t block_size;          /* forward-model threads per CTA */
     uint32_t particles_per_thread;/* independent walkers interleaved per thread: 1, 2 or 4 */
-    uint32_t hist_tile_rows;      /* histogram rows privatised in shared memory */
+    uint32_t hist_tile_rows;      /* histogram rows privatised in shared memory.  0 (default):
+                                   * none; records are global atomics and each warp takes its
+                                   * own 32-particle slices of the work items (no CTA barrier) */
     uint32_t warp_aggregate;      /* 1: warp-aggregated shared atomics, 0: plain */
     uint32_t chunk_particles;     /* particles per work item */
     uint32_t round_capacity;      /* proposals per batched round */

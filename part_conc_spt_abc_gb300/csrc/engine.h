@@ -52,7 +52,7 @@ struct DevBuf {
 struct Tuning {
     uint32_t block = 256;
     uint32_t ppt = 1;
-    uint32_t tile_rows = 64;
+    uint32_t tile_rows = 0; /* 0: no shared-memory tile, warps take their own slices of the items */
     uint32_t aggregate = 0;
     uint32_t chunk = 256;
     uint32_t capacity = 2048;
