@@ -153,9 +153,11 @@ def config3(ctx, seed=0, generations=10):
 
 def serve_stream(ctx, n_jobs=64, seed=0, rate_per_s=2.0, pop_range=(256, 4096), gen_range=(6, 12),
                  frames_range=(100, 500), bins_range=(64, 256), videos=20):
-    """Jobs of the serving stream and their arrival offsets (seconds)."""
+    """Jobs of the serving stream and their arrival offsets (seconds).  At
+    least 64 arrival gaps are drawn before the jobs, so a shorter stream's
+    jobs are the first jobs of the 64-job stream."""
     rng = np.random.default_rng(seed)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, n_jobs))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, max(n_jobs, 64)))[:n_jobs]
     arrivals -= arrivals[0]
     jobs = []
     for j in range(n_jobs):
