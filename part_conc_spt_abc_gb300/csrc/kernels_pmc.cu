@@ -436,16 +436,17 @@ __global__ void __launch_bounds__(1024) k_accept(PmcArgs a)
 /* whitened coordinates for the kernel density: y = A^-1 (theta - mean),
  * A = diag(tau) or the Cholesky factor; fixed parameters dropped.  Output
  * float [2][N][P] in the job's ybuf (old population, then new). */
-__global__ void k_whiten(PmcArgs a)
+__device__ __forceinline__ bool needs_kernel_sum_(const JobPmcDev& pm)
 {
-    const uint32_t j = blockIdx.y;
-    if (j >= a.round->n_jobs) return;
-    JobPmcDev& pm = a.pmc[j];
-    if (pm.done || !pm.gen_ended || pm.generation == 0u || pm.weighting != 0u) return;
-    if ((double)pm.trials >= (double)pm.avg_trials * (double)pm.N) return;
+    return !(pm.done || !pm.gen_ended || pm.generation == 0u || pm.weighting != 0u) &&
+           !((double)pm.trials >= (double)pm.avg_trials * (double)pm.N);
+}
+
+/* y_i = L^-1 (theta_i - lo) (Cholesky) or (theta_i - lo) / tau: point i of
+ * the committed (i < N) or new (i >= N) population, whitened. */
+__device__ __forceinline__ void whiten_one_(const JobPmcDev& pm, uint32_t i)
+{
     const uint32_t N = pm.N, P = pm.P;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 2u * N) return;
     const double* th = (i < N) ? pm.theta + (uint64_t)i * P : pm.theta_new + (uint64_t)(i - N) * P;
     float* y = pm.ybuf + (uint64_t)i * P;
     double v[PCS_MAX_P];
@@ -467,20 +468,42 @@ __global__ void k_whiten(PmcArgs a)
     for (uint32_t p = 0; p < P; ++p) y[p] = (float)v[p];
 }
 
+/* The grid covers one job's 2N points and strides over the round's jobs, so
+ * rounds that end no generation launch a few blocks that return at once. */
+__global__ void k_whiten(PmcArgs a)
+{
+    const uint32_t n_jobs = a.round->n_jobs;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        const JobPmcDev& pm = a.pmc[j];
+        if (!needs_kernel_sum_(pm)) continue;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < 2u * pm.N; i += gridDim.x * blockDim.x)
+            whiten_one_(pm, i);
+    }
+}
+
+
 /* pmc-standard (simulation_impl.inl:832-871): log w*_a = -log sum_i w_i
  * exp(-0.5 |y*_a - y_i|^2) (the Gaussian normalising constants cancel in
  * the normalisation).  One warp per new particle a. */
+__device__ __forceinline__ void kernel_sum_one_(const JobPmcDev& pm, uint32_t an, uint32_t lane);
+
 __global__ void __launch_bounds__(256) k_kernel_sum(PmcArgs a)
 {
-    const uint32_t j = blockIdx.y;
-    if (j >= a.round->n_jobs) return;
-    JobPmcDev& pm = a.pmc[j];
-    if (pm.done || !pm.gen_ended || pm.generation == 0u || pm.weighting != 0u) return;
-    if ((double)pm.trials >= (double)pm.avg_trials * (double)pm.N) return;
-    const uint32_t N = pm.N, P = pm.P;
+    const uint32_t n_jobs = a.round->n_jobs;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t an = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (an >= N) return;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        const JobPmcDev& pm = a.pmc[j];
+        if (!needs_kernel_sum_(pm)) continue;
+        for (uint32_t an = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; an < pm.N; an += warps)
+            kernel_sum_one_(pm, an, lane);
+    }
+}
+
+/* log w*_an for new particle an, one warp */
+__device__ __forceinline__ void kernel_sum_one_(const JobPmcDev& pm, uint32_t an, uint32_t lane)
+{
+    const uint32_t N = pm.N, P = pm.P;
     const float* yb = pm.ybuf;
     const float* ya = yb + (uint64_t)(N + an) * P;
     float yl[PCS_MAX_P];
@@ -588,9 +611,12 @@ __device__ void start_generation_(JobPmcDev& pm)
 }
 
 /* finalize: one block per job whose generation ended this round */
+constexpr uint32_t kWcumChunk = 1024;
+
 __global__ void __launch_bounds__(1024) k_finalize(PmcArgs a)
 {
     __shared__ double s_red[32];
+    __shared__ double s_wc[kWcumChunk];
     __shared__ double s_sel;
     __shared__ double s_mean[PCS_MAX_P];
     __shared__ double s_cov[PCS_MAX_P * PCS_MAX_P];
@@ -656,12 +682,24 @@ __global__ void __launch_bounds__(1024) k_finalize(PmcArgs a)
         __syncthreads();
     }
 
-    /* cumulative weights (partial_sum, :222); single thread keeps the order */
-    if (tid == 0) {
-        double acc = 0.0;
-        for (uint32_t i = 0; i < N; ++i) {
-            acc += pm.w[i];
-            pm.wcum[i] = acc;
+    /* cumulative weights (partial_sum, :222): one thread adds them in the
+     * reference's order, from a shared-memory copy of each 1024-weight chunk
+     * (a chain through global memory would wait for every load in turn) */
+    {
+        double acc = 0.0; /* thread 0's running sum across chunks */
+        for (uint32_t base = 0; base < N; base += kWcumChunk) {
+            const uint32_t m = min(kWcumChunk, N - base);
+            for (uint32_t i = tid; i < m; i += bd) s_wc[i] = pm.w[base + i];
+            __syncthreads();
+            if (tid == 0) {
+                for (uint32_t i = 0; i < m; ++i) {
+                    acc += s_wc[i];
+                    s_wc[i] = acc;
+                }
+            }
+            __syncthreads();
+            for (uint32_t i = tid; i < m; i += bd) pm.wcum[base + i] = s_wc[i];
+            __syncthreads();
         }
     }
     /* perturbation factor from the (new) committed population */
@@ -833,10 +871,9 @@ cudaError_t launch_accept(const PmcArgs& a, uint32_t n_jobs, cudaStream_t st)
 
 cudaError_t launch_finalize(const PmcArgs& a, uint32_t n_jobs, uint32_t max_n, cudaStream_t st)
 {
-    dim3 gw((2u * max_n + 255) / 256, n_jobs);
-    k_whiten<<<gw, 256, 0, st>>>(a);
-    dim3 gk((max_n * 32u + 255) / 256, n_jobs);
-    k_kernel_sum<<<gk, 256, 0, st>>>(a);
+    /* grids for one job's points; the kernels stride over the round's jobs */
+    k_whiten<<<(2u * max_n + 255) / 256, 256, 0, st>>>(a);
+    k_kernel_sum<<<(max_n * 32u + 255) / 256, 256, 0, st>>>(a);
     k_finalize<<<n_jobs, 1024, 0, st>>>(a);
     return cudaGetLastError();
 }
