@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Benchmark of the ABC-PMC hot path on GB300.
 
-Workload (BASELINE configuration 1): two-component lognormal mixture
+Workload (configuration 1): two-component lognormal mixture
 (175/500 nm, sd 10/25 nm, weights 0.6/0.4, 5e14 m^-3), 50 videos x 300
 frames, population 1024, epsilon = 50% quantile, histograms 301 x 128.  A
 step is one ABC-PMC generation (batched rounds until every population slot
@@ -257,7 +257,7 @@ def plain_stream_run(P, ctx, jobs, arrivals, budget_s, geometry):
 
 
 def run_serve(args, rank, world):
-    """The serving stream (BASELINE configuration 4): jobs arrive as a
+    """The serving stream (configuration 4): jobs arrive as a
     Poisson process at 2 jobs/s.  The served form admits them into the
     continuous-batching loop as they arrive (headline: p50/p99 latency and
     accepted proposals/s over the whole stream).  The plain form runs jobs
@@ -266,7 +266,7 @@ def run_serve(args, rank, world):
     ratio is taken on equal work at saturation: the first --cmp-jobs jobs of
     the stream, each capped at --cmp-generations generations after the prior
     pass, all submitted at time 0, run by the plain form (one job after
-    another; reference launch geometry, and this build's persistent grid)
+    another; reference launch geometry, and the library's persistent grid)
     and by the served form (all jobs at once)."""
     import part_conc_spt_abc_gb300 as P
     import part_conc_spt_abc_gb300.workloads as W
@@ -306,7 +306,7 @@ def run_serve(args, rank, world):
                                      f"prior pass each, all submitted at time 0, plain budget "
                                      f"{args.plain_budget:.0f} s per form",
                        "plain_forms": "reference_launch: ceil(V/4) CTAs x 128 threads per proposal, as the "
-                                      "reference launches its kernel; persistent_grid: this build's grid"},
+                                      "reference launches its kernel; persistent_grid: the library's persistent grid"},
             **res}
     print(json.dumps(line), flush=True)
     ctx.close()

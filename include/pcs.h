@@ -42,7 +42,7 @@ typedef enum pcs_status {
     PCS_ERR_CUDA = 2,             /* a CUDA runtime call failed (error::CudaError) */
     PCS_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed or admission refused */
     PCS_ERR_XML = 4,              /* input/data/output XML problem (error::XMLLoadError) */
-    PCS_ERR_UNSUPPORTED = 5,      /* valid request this build does not implement */
+    PCS_ERR_UNSUPPORTED = 5,      /* valid request this library does not implement */
     PCS_ERR_DEVICE = 6,           /* a kernel raised its error word (bounds or timeout) */
     PCS_ERR_BUSY = 7,             /* the object is in use by a running call */
     PCS_ERR_NOT_FOUND = 8         /* unknown job / no result yet */
@@ -149,7 +149,7 @@ typedef struct pcs_tuning {
     uint32_t use_graphs;          /* 1: capture rounds in CUDA graphs, 0: direct launches */
     uint32_t plain_launch;        /* pcs_job_run_plain's simulate launch: 1 the reference's
                                    * geometry (ceil(V/4) CTAs x 128 threads per proposal,
-                                   * default), 2 this build's persistent grid */
+                                   * default), 2 the library's persistent grid */
     uint32_t round_fill;          /* a round whose proposals would carry fewer particles than
                                    * this (the end of a generation) gives its pending slots
                                    * proportionally more trials, up to the capacity.  Default:
@@ -217,7 +217,7 @@ pcs_status pcs_job_run(pcs_job* job, uint32_t max_steps);
 /* The plain form: the reference's schedule (host-side PMC in double, one
  * proposal per simulate + distance launch, `queues` streams in flight, at most
  * one trial per population slot in flight; src/gpu/detail/simulation_impl.inl
- * :178-455) on this build's kernels.  For comparison with pcs_job_run. */
+ * :178-455) on this library's kernels.  For comparison with pcs_job_run. */
 pcs_status pcs_job_run_plain(pcs_job* job, uint32_t max_steps, uint32_t queues);
 /* Advances a job by one generation (batched rounds until every slot is
  * accepted or the trial cap is hit).  *done becomes 1 when it has finished. */

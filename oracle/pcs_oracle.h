@@ -1,8 +1,8 @@
 /*
  * pcs_oracle.h -- CPU restatement of the reference's ABC-PMC hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA
- * implementation in part_conc_spt_abc_gb300/csrc: it is loaded by tests/,
+ * TEST INFRASTRUCTURE ONLY.  The tests compare the CUDA implementation in
+ * part_conc_spt_abc_gb300/csrc against this library: it is loaded by tests/,
  * by __graft_entry__.smoke() and by the cpu_baseline leg of bench.py, and by
  * nothing else.  The product never links, loads or calls it.
  *
@@ -39,7 +39,7 @@ extern "C" {
 enum {
     ORC_MODEL_DISCRETE_FIXED_Z = 0,    /* EModel::discreteFixedZ    (shared/common.hpp:11) */
     ORC_MODEL_DISCRETE_VARIABLE_Z = 1, /* EModel::discreteVariableZ (shared/common.hpp:12) */
-    ORC_MODEL_LOGNORMAL = 2            /* per-particle lognormal diameter (this build's model layer) */
+    ORC_MODEL_LOGNORMAL = 2            /* per-particle lognormal diameter (the library's model layer) */
 };
 
 /* cusim::SimulateSetup (kernel-simulate.cuh:19-38) plus the recorder's bin

@@ -81,7 +81,7 @@ void help(FILE* f, const char* self)
     std::fprintf(f,
                  "\ngpuspec is a comma separated list of GPU IDs (as shown by --list-devices).\n"
                  "Optionally, a queue count can be added to each GPU ID by appending a \"/N\".\n"
-                 "This build runs on the first listed GPU.\n"
+                 "accel runs on the first listed GPU.\n"
                  "\n(*) If specified, the -d/-o options override the paths given in the input XML\n"
                  "    for the data and for the output XML, respectively.\n");
 }
@@ -164,7 +164,7 @@ std::pair<int, int> parse_gpuspec(const std::string& spec, int verbosity)
             first_dev = (int)dev - 1;
             first_q = (int)(q ? q : 1);
         } else if (verbosity >= 0) {
-            std::fprintf(stderr, "Note: this build uses one GPU; ignoring GPU %u in gpuspec\n", dev);
+            std::fprintf(stderr, "Note: accel uses one GPU; ignoring GPU %u in gpuspec\n", dev);
         }
         ++count;
         const char* x = std::strchr(s, ',');
@@ -210,7 +210,7 @@ int main(int argc, char** argv)
             return 0;
         }
         if (cfg.dev_scalar == 'd')
-            throw CliError("std::runtime_error", "Device scalar type double is not supported by this build (the forward model computes in float)");
+            throw CliError("std::runtime_error", "Device scalar type double is not supported (the forward model computes in float)");
         if (cfg.host_scalar == 'f' && cfg.verbosity >= 0)
             std::fprintf(stderr, "Note: -hs f accepted; the population is kept in double\n");
         const auto gs = parse_gpuspec(cfg.gpu_spec, cfg.verbosity);

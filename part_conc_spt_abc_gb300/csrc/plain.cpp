@@ -1,5 +1,5 @@
 /*
- * plain.cpp -- the plain form: the reference's schedule on this build's
+ * plain.cpp -- the plain form: the reference's schedule on this library's
  * kernels.
  *
  * SimulationT::run (src/gpu/detail/simulation_impl.inl:178-455) keeps the

@@ -172,7 +172,7 @@ def xml_cases():
         if name == "input_empty_list.xml":
             # a whitespace-only list has no text node; input.cpp:241-260 then
             # hands a null pointer to strtoull and the reference crashes, so
-            # there is nothing to record (this build reports an XML error)
+            # there is nothing to record (the library reports an XML error)
             res[name] = {"data": os.path.basename(data), "ref": {"crash": True}}
             continue
         res[name] = {"data": os.path.basename(data), "ref": ref_input_load(inp, data)}

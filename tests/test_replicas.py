@@ -46,7 +46,7 @@ def test_gloo_max_and_sum_over_two_ranks(tmp_path):
 
 
 def test_reference_arm_under_torchrun_prints_one_line():
-    """bench.py --impl reference launched as the driver launches it for N=2:
+    """bench.py --impl reference launched through torchrun for N=2:
     rank 0 alone times the CPU reference and prints one JSON line; the
     other rank exits 0."""
     pytest.importorskip("torch")
