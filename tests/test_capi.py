@@ -50,3 +50,38 @@ def test_open_without_gpu_fails_cleanly(pcs):
     st = pcs.lib().pcs_open(0, 0, C.byref(h))
     assert st != 0 and not h.value
     assert pcs.lib().pcs_last_error()
+
+
+STRUCTS = {"Params": "pcs_params", "Observed": "pcs_observed", "Tuning": "pcs_tuning", "JobInfo": "pcs_job_info",
+           "KernelStats": "pcs_kernel_stats", "Setup": "pcs_setup", "Run": "pcs_run", "Replay": "pcs_replay",
+           "OutputMeta": "pcs_output_meta", "OutputView": "pcs_output_view"}
+
+
+def test_ctypes_mirrors_match_the_header_layout(pcs, tmp_path):
+    """Every ctypes structure of the Python binding has the size and field
+    offsets that a C compiler gives the struct of include/pcs.h."""
+    import shutil
+    import pytest
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "pcs.h"', "int main(void) {"]
+    for py, cname in STRUCTS.items():
+        cls = getattr(pcs._lib, py)
+        lines.append(f'  printf("{py} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("{py} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        py, field, value = line.split()
+        got[(py, field)] = int(value)
+    for py in STRUCTS:
+        cls = getattr(pcs._lib, py)
+        assert got[(py, "size")] == C.sizeof(cls), py
+        for f, _ in cls._fields_:
+            assert got[(py, f)] == getattr(cls, f).offset, (py, f)
