@@ -49,13 +49,19 @@ OPS_SPLIT_TASK = 312
 DIST_BYTES_PER_CELL = 12
 WORKLOAD = ("config1: 2-component lognormal (175/500 nm, sd 10/25, w 0.6/0.4), 5e14 m^-3, "
             "50 videos x 300 frames, pop 1024, quantile-0.5 schedule, R x B = 301 x 128")
+# generation cap of each configuration's jobs (prior pass not counted)
+GENERATIONS = {0: 8, 1: 12, 2: 8, 3: 10}
+STEP_SEQ = ("one ABC-PMC generation (the prior pass counts as one) of a sequence of jobs run back to back, seeds "
+            "1, 2, ..., each ended by its cap of {g} generations or by the trial cap (500 trials per slot on "
+            "average; that generation is discarded, as the reference discards it); every timed step ends a "
+            "generation that did work")
 WORKLOADS = {
     0: ("config0: 1-component lognormal (175 nm, sd 10), 2e14 m^-3, 20 videos x 200 frames, pop 256, "
-        "quantile-0.5 schedule, R x B = 201 x 100", "one ABC-PMC generation"),
-    1: (WORKLOAD, "one ABC-PMC generation"),
+        "quantile-0.5 schedule, R x B = 201 x 100", STEP_SEQ.format(g=GENERATIONS[0])),
+    1: (WORKLOAD, STEP_SEQ.format(g=GENERATIONS[1])),
     2: ("config2: 2-component lognormal, diameters U(100,800) nm, concentration prior spanning 50..5000 "
         "particles per video, 20 videos x 200 frames, pop 512, 512 proposals per round, R x B = 201 x 100",
-        "one ABC-PMC generation (512-proposal rounds)"),
+        STEP_SEQ.format(g=GENERATIONS[2]) + " (512-proposal rounds)"),
     3: ("config3: 3-component lognormal (100/250/600 nm, sd 5%, w 0.3/0.4/0.3), 1e5 particles per video, "
         "100 videos x 1000 frames, pop 4096, R x B = 1001 x 256",
         "one round of 64 prior-pass proposals (fixed slice; a full run is ~4e14 particle-steps)"),
@@ -312,6 +318,48 @@ def run_serve(args, rank, world):
     ctx.close()
 
 
+class JobSequence:
+    """Estimation jobs of one configuration run back to back (seeds seed0,
+    seed0 + 1, ...), each until its generation cap or the trial cap ends it.
+    step() advances the current job by one generation (its prior pass counts
+    as one; a generation that reaches the trial cap is discarded, as the
+    reference discards it, and ends the job), then moves on to the next job,
+    so every step ends a generation that did work.  `prepare` jobs are
+    created up front (their observed data uploaded); later ones on demand."""
+
+    def __init__(self, P, ctx, inp, seed0: int, prepare: int = 0):
+        self.P, self.ctx, self.inp, self.seed0 = P, ctx, inp, seed0
+        self.ready = [P.make_simulation(ctx, inp, seed0 + i) for i in range(prepare)]
+        self.made = prepare
+        self.cur = None
+        self.sims = []
+        self.jobs_finished = 0
+
+    def step(self):
+        if self.cur is None:
+            if self.ready:
+                self.cur = self.ready.pop(0)
+            else:
+                self.cur = self.P.make_simulation(self.ctx, self.inp, self.seed0 + self.made)
+                self.made += 1
+            self.sims.append(self.cur)
+        sim = self.cur
+        if sim.step():
+            self.cur = None
+            self.jobs_finished += 1
+        return sim
+
+    def totals(self):
+        """(particle-steps, proposals, accepted) of every job started."""
+        infos = [s.info() for s in self.sims]
+        return (sum(i.particle_steps for i in infos), sum(i.simulations for i in infos),
+                sum(i.accepted for i in infos))
+
+    def close(self):
+        for s in self.sims + self.ready:
+            s.close()
+
+
 def simulate_traffic(launch_ms: float):
     """DRAM bytes (read + write) of one k_simulate launch, from the ncu
     capture of a configuration-1 launch summarised in profiles/ (line
@@ -393,7 +441,7 @@ def main():
     ctx = P.Context(local)
     cfg = 0 if args.small else args.config
     workload, step_def = WORKLOADS[cfg]
-    gens = args.warmup + args.steps + 2
+    gens = GENERATIONS[cfg]
     inp, truth = {0: W.config0, 1: W.config1, 2: W.config2, 3: W.config3}[cfg](ctx, seed=0, generations=gens)
     if not args.no_autotune and cfg != 3:
         ctx.autotune(inp)
@@ -413,56 +461,78 @@ def main():
         run_plain_config(args, P, ctx, inp, workload, rank)
         return
 
-    def stepper(sim):
-        """advance one step: a generation, or one round of the fixed slice"""
-        if cfg != 3:
-            return sim.step
-        srv = P.Server(ctx)
-        srv.submit(sim)
-        return srv.step
+    class SliceSteps:
+        """configuration 3: one round of the fixed 64-proposal prior-pass slice per step"""
+
+        def __init__(self, seed):
+            self.sim = P.make_simulation(ctx, inp, seed)
+            self.srv = P.Server(ctx)
+            self.srv.submit(self.sim)
+            self.sims = [self.sim]
+            self.jobs_finished = 0
+
+        def step(self):
+            self.srv.step()
+            return self.sim
+
+        def totals(self):
+            i = self.sim.info()
+            return i.particle_steps, i.simulations, i.accepted
+
+        def close(self):
+            self.sim.close()
+
+    def sequence(seed0, prepare):
+        return SliceSteps(seed0) if cfg == 3 else JobSequence(P, ctx, inp, seed0, prepare)
 
     # ---- device-resident run: inputs already in HBM -----------------------
-    sim = P.make_simulation(ctx, inp, seed=1 + rank)
-    step = stepper(sim)
+    # every job the warm-up and the timed steps can need is created (its
+    # observed data uploaded) before the timed region
+    seq = sequence(1 + 1000 * rank, args.warmup + args.steps)
     for _ in range(args.warmup):
-        step()
+        seq.step()
     barrier(world)
     ctx.reset_kernel_stats()
-    i0 = sim.info()
+    t0_steps, t0_props, t0_acc = seq.totals()
+    jobs0 = seq.jobs_finished
     clocks = Clocks(local)
     ctx.timer_start()
     for _ in range(args.steps):
-        step()
+        seq.step()
     ms = ctx.timer_stop()
     clk = clocks.stop()
-    i1 = sim.info()
+    t1_steps, t1_props, t1_acc = seq.totals()
+    jobs_ended = seq.jobs_finished - jobs0
     ks = ctx.kernel_stats()
-    steps_local = i1.particle_steps - i0.particle_steps
-    props_local = i1.simulations - i0.simulations
-    acc_local = i1.accepted - i0.accepted
+    steps_local = t1_steps - t0_steps
+    props_local = t1_props - t0_props
+    acc_local = t1_acc - t0_acc
     ms_max = allreduce(ms, "max", world)
     steps_all = allreduce(float(steps_local), "sum", world)
     props_all = allreduce(float(props_local), "sum", world)
     acc_all = allreduce(float(acc_local), "sum", world)
     value = steps_all / (ms_max / 1e3)
-    sim.close()
+    seq.close()
 
     # ---- end to end through the public API, host buffers ------------------
+    # jobs are created inside the timed region here (H2D: observed K, DE,
+    # frame counts); each step reads the population back (D2H)
     barrier(world)
     t0 = time.perf_counter()
-    sim2 = P.make_simulation(ctx, inp, seed=101 + rank)  # H2D: observed K, DE, frame counts
-    step2 = stepper(sim2)
-    d2h = 0
+    seq2 = sequence(501 + 1000 * rank, 0)
+    d2h_total = 0
     for _ in range(args.steps):
-        step2()
+        sim2 = seq2.step()
         out = sim2.output()  # D2H: the population (m, s, c, az, dist, w)
-        d2h = sum(a.nbytes for a in (out.m, out.c, out.az, out.dist, out.w, out.s) if a is not None)
+        d2h_total += sum(a.nbytes for a in (out.m, out.c, out.az, out.dist, out.w, out.s) if a is not None)
     e2e_s = time.perf_counter() - t0
-    e2e_steps = sim2.info().particle_steps
-    sim2.close()
+    e2e_steps = seq2.totals()[0]
+    e2e_jobs = len(seq2.sims)
+    seq2.close()
     e2e_s = allreduce(e2e_s, "max", world)
     e2e_value = allreduce(float(e2e_steps), "sum", world) / e2e_s
-    h2d = (inp.K.nbytes + inp.DE.nbytes + inp.frames.nbytes) / args.steps
+    h2d = e2e_jobs * (inp.K.nbytes + inp.DE.nbytes + inp.frames.nbytes) / args.steps
+    d2h = d2h_total / args.steps
 
     # ---- roofline of the dominant kernel (forward model: issue bound) -----
     sim_ms = ks.simulate_ms / max(1, ks.simulate_launches)
@@ -490,7 +560,9 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload, "step": step_def, "parallelism": f"replicas x{world}",
-                   "l2": l2_note, "tuning": tune},
+                   "l2": l2_note, "tuning": tune,
+                   "timed_region": {"steps": args.steps, "generations_ended": int(ks.generations),
+                                    "jobs_ended": jobs_ended, "generation_cap": GENERATIONS[cfg]}},
         "proposals_per_s": props_all / (ms_max / 1e3),
         "accepted_per_s": acc_all / (ms_max / 1e3),
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
