@@ -385,13 +385,15 @@ pcs_status pcs_scan_distance(pcs_ctx* ctx, const uint32_t* hist, const uint32_t*
  * as K_distance resets its input; d_ref_sat is rows x bins; d_dist_f32 gets
  * count float distances in the reference kernel's reduction order.  Work is
  * queued on `stream` (a cudaStream_t, NULL = default stream) of the current
- * device; the call does not wait for it.  Limits: rows * bins <=
+ * device, and the call waits for it: it reads the kernel's error word back
+ * and returns PCS_ERR_DEVICE if the kernel raised it.  Limits: rows * bins <=
  * PCS_NOALLOC_MAX_CELLS and count <= PCS_NOALLOC_MAX_COUNT, else
  * PCS_ERR_INVALID_ARGUMENT.  The array (about 4.7 MiB) stays reserved on each
  * GPU that loads the library until exit.  The first call on a device looks
  * the array's address up (cudaGetSymbolAddress), so make it before any stream
- * capture.  All calls share the array: calls whose work overlaps on the GPU
- * race and must not be issued. */
+ * capture; the address is kept for the process's life, so the entry point
+ * does not survive cudaDeviceReset on that device.  All calls share the
+ * array: calls whose work overlaps on the GPU race and must not be issued. */
 #define PCS_NOALLOC_MAX_CELLS 1048576u
 #define PCS_NOALLOC_MAX_COUNT 4096u
 pcs_status pcs_scan_distance_noalloc(uint32_t* d_hist, const uint32_t* d_ref_sat, uint32_t rows,
@@ -412,6 +414,24 @@ pcs_status pcs_observed_sat_julia(pcs_ctx* ctx, const uint32_t* K, const double*
 pcs_status pcs_debug_particle_stream(pcs_ctx* ctx, uint64_t seed, uint32_t slot, uint32_t trial,
                                      uint32_t generation, uint32_t particle, uint32_t block,
                                      uint32_t out[4]);
+
+/* The proposals of the context's last batched round that belong to `job`
+ * (checks of the proposal construction, src/gpu/detail/simulation_impl.inl
+ * :256-347, which the reference builds on the host per proposal): for each,
+ * its slot, trial, generation, particle total and float forward-model
+ * arguments, its parameter vector theta [n][P] (sample layout [m | s
+ * (lognormal) | log10c | az]) and its particle counts [n][V].  They are
+ * valid until the next round; the job must still be in the round table (not
+ * retired).  With props NULL only *n is written. */
+typedef struct pcs_debug_proposal {
+    uint32_t slot, trial, generation, total_particles;
+    float half_az[PCS_MAX_COMPONENTS];
+    float pre_comp_prob[PCS_MAX_COMPONENTS];
+    float sd_scale[PCS_MAX_COMPONENTS];
+    float sd_shape[PCS_MAX_COMPONENTS];
+} pcs_debug_proposal;
+pcs_status pcs_debug_round_proposals(pcs_job* job, uint32_t cap, uint32_t* n, pcs_debug_proposal* props,
+                                     double* theta, uint32_t* counts);
 
 #ifdef __cplusplus
 }

@@ -10,9 +10,15 @@
  * pcs_oracle.c's conventions (GPU conventions, float walk, one thread per
  * slot at a time), the cumulative distance in the reference order, the
  * reference's double-precision pmc-standard weights and tau = sqrt(2 var).
- * Model: lognormal diameters (mean m, sd s) with Stokes-Einstein steps,
- * log10 concentrations, one fixed depth.  Schedule: epsilon = q-quantile of
- * the previous generation's distances (prior pass for the first).
+ * Models: lognormal diameters (mean m, sd s) with Stokes-Einstein steps,
+ * log10 concentrations, one fixed depth; or the reference's discrete
+ * diffusivities with one depth parameter (discrete-fixed-depth,
+ * simulation_impl.inl:178-455), whose prior pass uses az itself as the half
+ * depth when full_az_prior is set (:782).  Schedules: epsilon = q-quantile of
+ * the previous generation's distances (prior pass for the first), or the
+ * reference's gamma_0 = rank N/2 of the prior distances (:819-829) lowered
+ * by delta_gamma at the start of each generation (:202-219), with the trial
+ * cap discarding the generation that reaches it (:425-428).
  */
 #include <math.h>
 #include <stdio.h>
@@ -54,6 +60,7 @@ static void rn_seed(rng* r, uint64_t a, uint64_t b, uint64_t c)
         r->s[i] = z ^ (z >> 31);
     }
     r->have = 0;
+    r->spare = 0.0;
 }
 static inline double rn_n(rng* r)
 {
@@ -91,8 +98,11 @@ typedef struct ctx_t {
     double gamma;
     uint32_t gen;
     uint64_t seed;
+    uint32_t oc, oaz;  /* offsets of log10c and az in a parameter vector */
+    uint64_t trial_cap; /* trials per generation at which it is discarded (0: none) */
     atomic_uint next;
     atomic_ullong trials;
+    atomic_ullong gen_trials;
 } ctx_t;
 
 /* forward model of one proposal, GPU conventions (pcs_oracle.c) */
@@ -101,9 +111,10 @@ static double simulate_distance(const ctx_t* c, const double* th, rng* r, uint32
     const orc_abc_problem* pb = c->pb;
     const uint32_t C = pb->C;
     memset(hist, 0, sizeof(uint32_t) * (size_t)pb->R * pb->B);
+    const int lognormal = pb->model == ORC_MODEL_LOGNORMAL;
     double csum = 0.0, powc[ORC_MAX_COMPONENTS];
     for (uint32_t i = 0; i < C; ++i) {
-        powc[i] = pow(10.0, th[2 * C + i]);
+        powc[i] = pow(10.0, th[c->oc + i]);
         csum += powc[i];
     }
     float pre[ORC_MAX_COMPONENTS];
@@ -116,15 +127,22 @@ static double simulate_distance(const ctx_t* c, const double* th, rng* r, uint32
     const double kB = 1.380649e-23;
     const double g = sqrt(2.0 * pb->deltat * kB * pb->temperature * 1e21 / (3.0 * M_PI * pb->viscosity));
     double mul[ORC_MAX_COMPONENTS], sl[ORC_MAX_COMPONENTS];
+    float sd_fixed[ORC_MAX_COMPONENTS];
     for (uint32_t i = 0; i < C; ++i) {
-        const double mu = th[i], sd = th[C + i];
-        const double s2 = log1p(sd * sd / (mu * mu));
-        sl[i] = sqrt(s2);
-        mul[i] = log(mu) - 0.5 * s2;
+        if (lognormal) {
+            const double mu = th[i], sd = th[C + i];
+            const double s2 = log1p(sd * sd / (mu * mu));
+            sl[i] = sqrt(s2);
+            mul[i] = log(mu) - 0.5 * s2;
+        } else {
+            sd_fixed[i] = (float)sqrt(2.0 * th[i] * pb->deltat); /* randWalkStddev (:337-340) */
+        }
     }
     const double lambda = csum * pb->Lx * pb->Ly * pb->Lz / 1e12;
     const float hlx = 0.5f * (float)pb->Lx, hly = 0.5f * (float)pb->Ly, hlz = 0.5f * (float)pb->Lz;
-    const float hax = 0.5f * (float)pb->ax, hay = 0.5f * (float)pb->ay, haz = 0.5f * (float)pb->az;
+    const float hax = 0.5f * (float)pb->ax, hay = 0.5f * (float)pb->ay;
+    const float azf = (float)th[c->oaz];
+    const float haz = (c->gen == 0 && pb->full_az_prior && !lognormal) ? azf : 0.5f * azf;
     const float four_dt = 4.0f * (float)pb->deltat, dde = (float)(pb->ub_de / pb->B);
     for (uint32_t v = 0; v < pb->V; ++v) {
         /* rand_poisson.jl: exponential gaps */
@@ -143,7 +161,7 @@ static double simulate_distance(const ctx_t* c, const double* th, rng* r, uint32
             const float u = (float)rn_u(r);
             uint32_t idx = 0;
             while (idx + 1 < C && pre[idx] <= u) ++idx;
-            const float sd = (float)(g * exp(-0.5 * (mul[idx] + sl[idx] * rn_n(r))));
+            const float sd = lognormal ? (float)(g * exp(-0.5 * (mul[idx] + sl[idx] * rn_n(r)))) : sd_fixed[idx];
             float de = 0.0f;
             uint32_t k = (fabsf(z) <= haz && fabsf(x) <= hax && fabsf(y) <= hay) ? 1u : 0u;
             for (uint32_t f = 1; f < F; ++f) {
@@ -200,10 +218,11 @@ static void propose(const ctx_t* c, rng* r, double* th)
         }
         th[p] = orc_displace(c->theta[(size_t)parent * P + p], c->tau[p] * rn_n(r), c->lo[p], c->hi[p]);
     }
-    /* sort components by mean diameter */
+    /* sort components by m, their other per-component parameters with them */
+    const uint32_t groups = c->oc / C + 1;
     for (uint32_t i = 1; i < C; ++i)
         for (uint32_t x = i; x > 0 && th[x] < th[x - 1]; --x)
-            for (uint32_t g = 0; g < 3; ++g) {
+            for (uint32_t g = 0; g < groups; ++g) {
                 double t = th[g * C + x];
                 th[g * C + x] = th[g * C + x - 1];
                 th[g * C + x - 1] = t;
@@ -229,7 +248,8 @@ static void* slot_worker(void* arg)
                 propose(c, &r, th);
             const double d = simulate_distance(c, th, &r, hist);
             atomic_fetch_add(&c->trials, 1ull);
-            if (c->gen == 0 || d <= c->gamma || t > 200000) {
+            const uint64_t gt = atomic_fetch_add(&c->gen_trials, 1ull) + 1ull;
+            if (c->gen == 0 || d <= c->gamma || t > 200000 || (c->trial_cap && gt >= c->trial_cap)) {
                 memcpy(c->theta_new + (size_t)s * P, th, sizeof(double) * P);
                 c->dist_new[s] = d;
                 break;
@@ -258,26 +278,38 @@ static double quantile_of(const double* d, uint32_t N, double q)
     return v;
 }
 
-/* Runs the estimation; theta_out [N * (3C+1)] (layout m | s | log10c | az),
- * w_out [N].  Returns the total number of trials. */
+/* Runs the estimation; theta_out [N * P] (layout m | s | log10c | az for
+ * the lognormal model, m | log10c | az for the discrete one), w_out [N].
+ * Returns the total number of trials. */
 uint64_t orc_abc_pmc(const orc_abc_problem* pb, uint64_t seed, uint32_t nthreads, double* theta_out,
-                     double* w_out)
+                     double* w_out, uint32_t* generations_out, int* converged_out)
 {
     ctx_t c;
     memset(&c, 0, sizeof c);
     c.pb = pb;
-    const uint32_t C = pb->C, N = pb->N, P = 3 * C + 1;
+    const int lognormal = pb->model == ORC_MODEL_LOGNORMAL;
+    const uint32_t C = pb->C, N = pb->N, P = (lognormal ? 3 : 2) * C + 1;
+    if (P > OP_MAXP || C > ORC_MAX_COMPONENTS) return 0;
     c.P = P;
     c.seed = seed;
+    c.oc = lognormal ? 2 * C : C;
+    c.oaz = c.oc + C;
     for (uint32_t i = 0; i < C; ++i) {
         c.lo[i] = pb->lb_m;
         c.hi[i] = pb->ub_m;
-        c.lo[C + i] = pb->lb_s;
-        c.hi[C + i] = pb->ub_s;
-        c.lo[2 * C + i] = log10(pb->lb_c);
-        c.hi[2 * C + i] = log10(pb->ub_c);
+        if (lognormal) {
+            c.lo[C + i] = pb->lb_s;
+            c.hi[C + i] = pb->ub_s;
+        }
+        c.lo[c.oc + i] = log10(pb->lb_c);
+        c.hi[c.oc + i] = log10(pb->ub_c);
     }
-    c.lo[3 * C] = c.hi[3 * C] = pb->az;
+    if (lognormal) {
+        c.lo[c.oaz] = c.hi[c.oaz] = pb->az;
+    } else {
+        c.lo[c.oaz] = pb->lb_az;
+        c.hi[c.oaz] = pb->ub_az;
+    }
     c.theta = (double*)malloc(sizeof(double) * N * P);
     c.theta_new = (double*)malloc(sizeof(double) * N * P);
     c.w = (double*)malloc(sizeof(double) * N);
@@ -293,8 +325,15 @@ uint64_t orc_abc_pmc(const orc_abc_problem* pb, uint64_t seed, uint32_t nthreads
     if (nthreads < 1) nthreads = 1;
     pthread_t* th = (pthread_t*)calloc(nthreads, sizeof(pthread_t));
     double* wstar = (double*)malloc(sizeof(double) * N);
+    uint32_t committed = 0;
+    int converged = 0;
+    int fixed[OP_MAXP] = {0};
+    for (uint32_t p = 0; p < P; ++p) fixed[p] = c.lo[p] == c.hi[p];
     for (uint32_t gen = 0; gen <= pb->generations; ++gen) {
         c.gen = gen;
+        if (gen > 0 && pb->schedule == 0) c.gamma -= pb->delta_gamma;
+        c.trial_cap = (gen > 0 && pb->avg_trials) ? (uint64_t)pb->avg_trials * N : 0ull;
+        atomic_store(&c.gen_trials, 0ull);
         /* tau from the current population (compute_tau_) */
         for (uint32_t p = 0; p < P; ++p) c.tau[p] = sqrt(2.0 * orc_var_uncorrected(c.theta + p, N, P));
         double acc = 0.0;
@@ -305,18 +344,25 @@ uint64_t orc_abc_pmc(const orc_abc_problem* pb, uint64_t seed, uint32_t nthreads
         atomic_store(&c.next, 0u);
         for (uint32_t t = 0; t < nthreads; ++t) pthread_create(&th[t], NULL, slot_worker, &c);
         for (uint32_t t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+        if (c.trial_cap && atomic_load(&c.gen_trials) >= c.trial_cap) {
+            converged = 1; /* the generation that reached the trial cap is discarded */
+            break;
+        }
         if (gen == 0) {
             memcpy(c.dist, c.dist_new, sizeof(double) * N);
         } else {
-            /* pmc-standard weights (simulation_impl.inl:832-871), fixed depth skipped */
-            int fixed[OP_MAXP] = {0};
-            fixed[3 * C] = 1;
+            /* pmc-standard weights (simulation_impl.inl:832-871), fixed parameters skipped */
             orc_weights_pmc_standard(c.theta_new, c.theta, c.w, c.tau, fixed, N, P, wstar);
             memcpy(c.w, wstar, sizeof(double) * N);
             memcpy(c.theta, c.theta_new, sizeof(double) * N * P);
             memcpy(c.dist, c.dist_new, sizeof(double) * N);
+            committed += 1;
         }
-        c.gamma = quantile_of(c.dist, N, pb->quantile);
+        if (pb->schedule == 0) {
+            if (gen == 0) c.gamma = quantile_of(c.dist, N, 0.5); /* rank N/2: the upper median */
+        } else {
+            c.gamma = quantile_of(c.dist, N, pb->quantile);
+        }
         if (getenv("PCS_ORACLE_TRACE")) {
             double ess = 0.0, s2 = 0.0;
             for (uint32_t i = 0; i < N; ++i) s2 += c.w[i] * c.w[i];
@@ -327,6 +373,8 @@ uint64_t orc_abc_pmc(const orc_abc_problem* pb, uint64_t seed, uint32_t nthreads
     }
     memcpy(theta_out, c.theta, sizeof(double) * N * P);
     memcpy(w_out, c.w, sizeof(double) * N);
+    if (generations_out) *generations_out = committed;
+    if (converged_out) *converged_out = converged;
     const uint64_t trials = atomic_load(&c.trials);
     free(th);
     free(wstar);

@@ -22,4 +22,7 @@ srcs=("$here/ref_harness.cpp"
       "$ref/src/gpu/support/cuda_error.cpp"
       "$ref/external/tinyxml2/tinyxml2.cpp")
 "$CXX" "${flags[@]}" -shared -o "$out/libpcsref.so" "${srcs[@]}"
+# the tree these were compiled from, for the scripts that read its fixtures
+# (oracle.reference_root())
+printf '%s\n' "$ref" > "$out/reference_root"
 echo "built $out/libpcsref.so"

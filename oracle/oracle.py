@@ -68,6 +68,22 @@ def build(quiet: bool = True) -> None:
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-s", "-C", HERE], check=True, stdout=out)
     subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, stdout=out)
+    subprocess.run(["bash", os.path.join(HERE, "build_ref_kdist.sh"), "prepare"], check=True, stdout=out)
+
+
+def reference_root():
+    """The reference tree: $PCS_REFERENCE_ROOT, else the tree build_ref.sh
+    compiled oracle/_ref from (recorded in oracle/_ref/reference_root), else
+    None.  Only fixture scripts and host-side tests use it."""
+    env = os.environ.get("PCS_REFERENCE_ROOT")
+    if env:
+        return env
+    try:
+        with open(os.path.join(HERE, "_ref", "reference_root")) as f:
+            root = f.read().strip()
+    except OSError:
+        return None
+    return root if root and os.path.isdir(root) else None
 
 
 _lib = None
@@ -329,25 +345,103 @@ class OrcAbcProblem(C.Structure):
         ("lb_c", C.c_double), ("ub_c", C.c_double), ("az", C.c_double), ("Lx", C.c_double), ("Ly", C.c_double),
         ("Lz", C.c_double), ("ax", C.c_double), ("ay", C.c_double), ("deltat", C.c_double), ("ub_de", C.c_double),
         ("temperature", C.c_double), ("viscosity", C.c_double), ("frames", _u32p), ("ref_sat", _u32p),
+        ("model", C.c_uint32), ("schedule", C.c_uint32), ("avg_trials", C.c_uint32), ("full_az_prior", C.c_uint32),
+        ("delta_gamma", C.c_double), ("lb_az", C.c_double), ("ub_az", C.c_double),
     ]
 
 
-def abc_pmc(problem: dict, frames, ref_sat, seed: int, nthreads: int):
-    """Whole ABC-PMC estimation on the CPU (abc_oracle.c).  Returns
-    (theta [N, 3C+1] with layout m | s | log10c | az, w [N], trials)."""
+def abc_pmc(problem: dict, frames, ref_sat, seed: int, nthreads: int, full: bool = False):
+    """Whole ABC-PMC estimation on the CPU (abc_oracle.c).  `problem` holds
+    OrcAbcProblem fields; model defaults to lognormal and schedule to the
+    quantile one.  Returns (theta [N, P] with layout m | s | log10c | az
+    (lognormal) or m | log10c | az (discrete), w [N], trials), plus
+    (generations committed, converged) when full."""
     L = lib()
-    L.orc_abc_pmc.argtypes = [C.POINTER(OrcAbcProblem), C.c_uint64, C.c_uint32, _f64p, _f64p]
+    L.orc_abc_pmc.argtypes = [C.POINTER(OrcAbcProblem), C.c_uint64, C.c_uint32, _f64p, _f64p,
+                              C.POINTER(C.c_uint32), C.POINTER(C.c_int)]
     L.orc_abc_pmc.restype = C.c_uint64
     fr = np.ascontiguousarray(frames, np.uint32)
     sat = np.ascontiguousarray(ref_sat, np.uint32)
     pb = OrcAbcProblem()
+    pb.model, pb.schedule = MODEL_LOGNORMAL, 1
     for k, v in problem.items():
         setattr(pb, k, v)
     pb.V, pb.R, pb.B = len(fr), sat.shape[0], sat.shape[1]
     pb.frames = ptr(fr, C.c_uint32)
     pb.ref_sat = ptr(sat, C.c_uint32)
-    P = 3 * problem["C"] + 1
+    P = (3 if pb.model == MODEL_LOGNORMAL else 2) * problem["C"] + 1
     th = np.zeros((problem["N"], P))
     w = np.zeros(problem["N"])
-    trials = L.orc_abc_pmc(C.byref(pb), seed, nthreads, ptr(th, C.c_double), ptr(w, C.c_double))
+    gens, conv = C.c_uint32(0), C.c_int(0)
+    trials = L.orc_abc_pmc(C.byref(pb), seed, nthreads, ptr(th, C.c_double), ptr(w, C.c_double), C.byref(gens),
+                           C.byref(conv))
+    if full:
+        return th, w, int(trials), int(gens.value), bool(conv.value)
     return th, w, int(trials)
+
+
+class OrcPropJob(C.Structure):
+    _fields_ = [("model", C.c_uint32), ("C", C.c_uint32), ("Z", C.c_uint32), ("P", C.c_uint32),
+                ("N", C.c_uint32), ("V", C.c_uint32), ("perturbation", C.c_uint32), ("full_az_prior", C.c_uint32),
+                ("seed", C.c_uint64), ("lo", C.c_double * 32), ("hi", C.c_double * 32),
+                ("volume_factor", C.c_double), ("delta_t", C.c_double), ("sd_const", C.c_double)]
+
+
+class OrcProposal(C.Structure):
+    _fields_ = [("parent", C.c_uint32), ("total_particles", C.c_uint32), ("lambda_", C.c_double),
+                ("half_az", C.c_float * MAXC), ("pre_comp_prob", C.c_float * MAXC),
+                ("sd_scale", C.c_float * MAXC), ("sd_shape", C.c_float * MAXC)]
+
+
+def prop_job(params, V: int, deltat: float, seed: int) -> OrcPropJob:
+    """orc_prop_job of a job with pcs_params-like `params` (attributes model,
+    component_count, abc_sample_count, perturbation, reference_initial_gamma,
+    Lx, Ly, Lz, lb_/ub_ m, s, c, az, temperature, viscosity)."""
+    import math
+    Cc = int(params.component_count)
+    model = int(params.model)
+    Z = Cc if model == MODEL_VARIABLE_Z else 1
+    lo, hi = [], []
+    lo += [params.lb_m] * Cc
+    hi += [params.ub_m] * Cc
+    if model == MODEL_LOGNORMAL:
+        lo += [params.lb_s] * Cc
+        hi += [params.ub_s] * Cc
+    lo += [math.log10(params.lb_c)] * Cc
+    hi += [math.log10(params.ub_c)] * Cc
+    lo += [params.lb_az] * Z
+    hi += [params.ub_az] * Z
+    j = OrcPropJob()
+    j.model, j.C, j.Z, j.P, j.N, j.V = model, Cc, Z, len(lo), int(params.abc_sample_count), V
+    j.perturbation = int(params.perturbation)
+    j.full_az_prior = 1 if (params.reference_initial_gamma and model != MODEL_LOGNORMAL) else 0
+    j.seed = seed
+    for i, (a, b) in enumerate(zip(lo, hi)):
+        j.lo[i], j.hi[i] = a, b
+    j.volume_factor = params.Lx * params.Ly * params.Lz / 1e12
+    j.delta_t = deltat
+    if model == MODEL_LOGNORMAL:
+        kB = 1.380649e-23
+        j.sd_const = math.sqrt(2.0 * deltat * kB * params.temperature * 1e21 / (3.0 * math.pi * params.viscosity))
+    return j
+
+
+def build_proposal(job: OrcPropJob, theta, wcum, factor, slot: int, trial: int, generation: int):
+    """(theta [P], counts [V], OrcProposal) of one proposal."""
+    L = lib()
+    if not getattr(L, "_prop_bound", False):
+        L.orc_build_proposal.argtypes = [C.POINTER(OrcPropJob), _f64p, _f64p, _f64p, C.c_uint32, C.c_uint32,
+                                         C.c_uint32, _f64p, _u32p, C.POINTER(OrcProposal)]
+        L.orc_build_proposal.restype = C.c_int
+        L._prop_bound = True
+    th = np.ascontiguousarray(theta, np.float64)
+    wc = np.ascontiguousarray(wcum, np.float64)
+    fa = np.ascontiguousarray(factor, np.float64)
+    out = np.zeros(job.P)
+    counts = np.zeros(max(1, job.V), np.uint32)
+    prop = OrcProposal()
+    rc = L.orc_build_proposal(C.byref(job), ptr(th, C.c_double), ptr(wc, C.c_double), ptr(fa, C.c_double), slot,
+                              trial, generation, ptr(out, C.c_double), ptr(counts, C.c_uint32), C.byref(prop))
+    if rc != 0:
+        raise ValueError(f"orc_build_proposal: {rc}")
+    return out, counts[:job.V], prop

@@ -762,3 +762,180 @@ int orc_weighted_cov_cholesky(const double* theta, const double* w, size_t N, si
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Proposal construction (simulation_impl.inl:256-347)                 */
+/* ------------------------------------------------------------------ */
+
+enum { STREAM_POISSON = 1u, STREAM_PERTURB = 2u, STREAM_PICK = 3u };
+
+/* one Philox block of a job's stream: counter (c0, tag << 28 | j,
+ * slot ^ m0, (generation << 20 | trial) ^ m1), fixed key */
+static void job_draw(uint64_t seed, uint32_t c0, uint32_t tag, uint32_t j, uint32_t slot, uint32_t gen,
+                     uint32_t trial, uint32_t w[4])
+{
+    const uint32_t key[2] = {0xA4093822u, 0x299F31D0u};
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const uint32_t ctr[4] = {c0, (tag << 28) | (j & 0x0FFFFFFFu), slot ^ (uint32_t)z,
+                             ((gen << 20) | (trial & 0xFFFFFu)) ^ (uint32_t)(z >> 32)};
+    orc_philox4x32_10(ctr, key, w);
+}
+
+/* [0,1) with 53 bits: 27 bits of the first word, 26 of the second */
+static double unit53(uint32_t a, uint32_t b)
+{
+    return (double)((((uint64_t)(a >> 5)) << 26) | (uint64_t)(b >> 6)) / 9007199254740992.0;
+}
+
+/* Poisson(lam) for one video.  lam < 12: inversion, one uniform.  lam >=
+ * 12: PTRS, the transformed rejection with squeeze of W. Hoermann, "The
+ * transformed rejection method for generating Poisson random variables",
+ * Insurance: Mathematics and Economics 12 (1993) 39-45, attempt t drawing
+ * (U, V) from block 1 + t; after 256 rejected attempts, round(lam). */
+static uint32_t poisson_video(uint64_t seed, double lam, uint32_t video, uint32_t slot, uint32_t gen,
+                              uint32_t trial)
+{
+    uint32_t w[4];
+    if (!(lam > 0.0)) return 0u;
+    if (lam < 12.0) {
+        job_draw(seed, video, STREAM_POISSON, 0u, slot, gen, trial, w);
+        const double u = unit53(w[0], w[1]);
+        double pk = exp(-lam), cdf = pk;
+        uint32_t k = 0;
+        while (cdf < u && k < 1000u) {
+            k += 1u;
+            pk = pk * (lam / (double)k);
+            cdf = cdf + pk;
+        }
+        return k;
+    }
+    const double b = 0.931 + 2.53 * sqrt(lam);
+    const double a = -0.059 + 0.02483 * b;
+    const double inv_alpha = 1.1239 + 1.1328 / (b - 3.4);
+    const double v_r = 0.9277 - 3.6224 / (b - 2.0);
+    for (uint32_t t = 0; t < 256u; ++t) {
+        job_draw(seed, video, STREAM_POISSON, 1u + t, slot, gen, trial, w);
+        const double U = unit53(w[0], w[1]) - 0.5;
+        const double V = unit53(w[2], w[3]);
+        const double us = 0.5 - fabs(U);
+        const double k = floor((2.0 * a / us + b) * U + lam + 0.43);
+        if (us >= 0.07 && V <= v_r) return (uint32_t)k;
+        if (k < 0.0) continue;
+        if (us < 0.013 && V > us) continue;
+        /* accept iff V inv_alpha / (a / us^2 + b) <= lam^k e^-lam / k!, in logs */
+        const double lhs = log(V) + log(inv_alpha) - log(a / (us * us) + b);
+        const double rhs = -lam + k * log(lam) - lgamma(k + 1.0);
+        if (lhs <= rhs) return (uint32_t)k;
+    }
+    return (uint32_t)floor(lam + 0.5);
+}
+
+int orc_build_proposal(const orc_prop_job* j, const double* theta, const double* wcum, const double* factor,
+                       uint32_t slot, uint32_t trial, uint32_t generation, double* theta_out,
+                       uint32_t* counts, orc_proposal* out)
+{
+    const uint32_t P = j->P, C = j->C, Z = j->Z, N = j->N;
+    if (P > 32 || C > ORC_MAX_COMPONENTS || Z > ORC_MAX_COMPONENTS || N == 0) return -1;
+    const int lognormal = j->model == ORC_MODEL_LOGNORMAL;
+    const uint32_t om = 0, os = C, oc = lognormal ? 2 * C : C, oaz = oc + C;
+    double th[32];
+    uint32_t w[4];
+    memset(out, 0, sizeof *out);
+    if (generation == 0u) {
+        memcpy(th, theta + (size_t)slot * P, P * sizeof(double));
+        out->parent = slot;
+    } else {
+        /* wrand_idx_: first cumulative weight not below U, at most N - 1 */
+        job_draw(j->seed, 0u, STREAM_PICK, 0u, slot, generation, trial, w);
+        const double u = unit53(w[0], w[1]);
+        uint32_t idx = N - 1u;
+        for (uint32_t i = 0; i < N; ++i)
+            if (!(wcum[i] < u)) {
+                idx = i;
+                break;
+            }
+        out->parent = idx;
+        /* normals, pair q/2 from one block: u1 in (0, 1], u2 in [0, 1) */
+        double n[32];
+        for (uint32_t q = 0; q < P; q += 2) {
+            job_draw(j->seed, q / 2u, STREAM_PERTURB, 0u, slot, generation, trial, w);
+            const double u1 = 1.0 - unit53(w[0], w[1]);
+            const double u2 = unit53(w[2], w[3]);
+            const double r = sqrt(-2.0 * log(u1));
+            n[q] = r * sin(2.0 * M_PI * u2);
+            if (q + 1 < P) n[q + 1] = r * cos(2.0 * M_PI * u2);
+        }
+        const double* parent = theta + (size_t)idx * P;
+        for (uint32_t p = 0; p < P; ++p) {
+            if (j->lo[p] == j->hi[p]) { /* a fixed parameter is not perturbed */
+                th[p] = j->lo[p];
+                continue;
+            }
+            double delta = 0.0;
+            if (j->perturbation == 1u) {
+                for (uint32_t i = 0; i <= p; ++i)
+                    if (j->lo[i] != j->hi[i]) delta += factor[p * P + i] * n[i];
+            } else {
+                delta = factor[p * P + p] * n[p];
+            }
+            th[p] = orc_displace(parent[p], delta, j->lo[p], j->hi[p]);
+        }
+        /* label switching: order the components by m (std::sort on indices) */
+        uint32_t order[ORC_MAX_COMPONENTS];
+        for (uint32_t i = 0; i < C; ++i) order[i] = i;
+        for (uint32_t i = 1; i < C; ++i)
+            for (uint32_t x = i; x > 0 && th[om + order[x]] < th[om + order[x - 1]]; --x) {
+                const uint32_t t = order[x];
+                order[x] = order[x - 1];
+                order[x - 1] = t;
+            }
+        double tmp[32];
+        memcpy(tmp, th, P * sizeof(double));
+        for (uint32_t i = 0; i < C; ++i) {
+            th[om + i] = tmp[om + order[i]];
+            th[oc + i] = tmp[oc + order[i]];
+            if (lognormal) th[os + i] = tmp[os + order[i]];
+            if (Z > 1u) th[oaz + i] = tmp[oaz + order[i]];
+        }
+    }
+    memcpy(theta_out, th, P * sizeof(double));
+
+    /* concentrations, Poisson mean, component probabilities, step sd */
+    double powc[ORC_MAX_COMPONENTS], csum = 0.0;
+    for (uint32_t i = 0; i < C; ++i) {
+        powc[i] = pow(10.0, th[oc + i]);
+        csum += powc[i];
+    }
+    const double lambda = csum * j->volume_factor;
+    out->lambda = lambda;
+    for (uint32_t i = 0; i < ORC_MAX_COMPONENTS; ++i) out->pre_comp_prob[i] = 2.0f;
+    double acc = 0.0;
+    for (uint32_t i = 0; i < C; ++i) {
+        acc += powc[i] / csum;
+        out->pre_comp_prob[i] = (float)acc;
+        if (lognormal) {
+            const double mu = th[om + i], sd = th[os + i];
+            const double sl2 = log1p((sd * sd) / (mu * mu));
+            const double mul = log(mu) - 0.5 * sl2;
+            out->sd_scale[i] = (float)(j->sd_const * exp(-0.5 * mul));
+            out->sd_shape[i] = (float)(-0.5 * sqrt(sl2));
+        } else {
+            out->sd_scale[i] = (float)sqrt(2.0 * th[om + i] * j->delta_t);
+        }
+    }
+    out->pre_comp_prob[C - 1] = 2.0f;
+    for (uint32_t z = 0; z < Z; ++z) {
+        const float az = (float)th[oaz + z];
+        out->half_az[z] = (generation == 0u && j->full_az_prior) ? az : 0.5f * az;
+    }
+    uint64_t total = 0;
+    for (uint32_t v = 0; v < j->V; ++v) {
+        counts[v] = poisson_video(j->seed, lambda, v, slot, generation, trial);
+        total += counts[v];
+    }
+    out->total_particles = total > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)total;
+    return 0;
+}

@@ -174,6 +174,44 @@ void orc_weights_inv_dist_sq(const double* dist, size_t N, double* w_out);
 int orc_weighted_cov_cholesky(const double* theta, const double* w, size_t N, size_t P,
                               double scale, double* cov, double* chol);
 
+/* One ABC-PMC proposal (simulation_impl.inl:256-347) drawn from the
+ * library's counter-based streams instead of the host std::mt19937:
+ * weighted parent pick (wrand_idx_ :54-62) on stream PICK, reflected
+ * Gaussian displacement of every free parameter (displace_ :64-79; the
+ * normals by Box-Muller from stream PERTURB, one counter per parameter pair;
+ * with a Cholesky factor, delta_p = sum_i<=p L[p][i] n_i), components sorted
+ * by m (:276-303, s and az moving with them), 10^log10c, lambda = sum c x
+ * volume factor (:305-306), one Poisson count per video (:310-317; stream
+ * POISSON, inversion below 12, Hoermann's PTRS above), the float forward-
+ * model arguments (:319-340).  Parameter layout [m | s (lognormal) | log10c
+ * | az].  Generation 0 (the prior pass) takes the slot's own parameters. */
+typedef struct orc_prop_job {
+    uint32_t model, C, Z, P, N, V;
+    uint32_t perturbation;      /* 0 diagonal tau, 1 lower Cholesky factor */
+    uint32_t full_az_prior;     /* prior pass uses the full az as half depth */
+    uint64_t seed;
+    double lo[32], hi[32];
+    double volume_factor;       /* Lx Ly Lz / 1e12 */
+    double delta_t;             /* discrete: step sd = sqrt(2 m dt) */
+    double sd_const;            /* lognormal: step sd = sd_const exp(-mu_ln / 2) at z = 0 */
+} orc_prop_job;
+
+typedef struct orc_proposal {
+    uint32_t parent;
+    uint32_t total_particles;
+    double lambda;
+    float half_az[ORC_MAX_COMPONENTS];
+    float pre_comp_prob[ORC_MAX_COMPONENTS];
+    float sd_scale[ORC_MAX_COMPONENTS];
+    float sd_shape[ORC_MAX_COMPONENTS];
+} orc_proposal;
+
+/* theta [N][P] committed population, wcum [N] cumulative weights, factor
+ * [P][P]; writes theta_out [P] and counts [V]. */
+int orc_build_proposal(const orc_prop_job* j, const double* theta, const double* wcum, const double* factor,
+                       uint32_t slot, uint32_t trial, uint32_t generation, double* theta_out,
+                       uint32_t* counts, orc_proposal* out);
+
 /* CPU baseline: the Julia forward model (src/cpu/simulate.jl) in Float64,
  * timed over many proposals on nthreads host threads (cpu_baseline.c). */
 typedef struct orc_cpu_job {
@@ -192,8 +230,16 @@ typedef struct orc_cpu_job {
 uint64_t orc_cpu_forward_batch(const orc_cpu_job* jobs, uint32_t n_jobs, uint32_t nthreads,
                                uint64_t seed, double* seconds, uint64_t* checksum);
 
-/* An independent CPU run of a whole ABC-PMC estimation (abc_oracle.c):
- * lognormal model, quantile schedule, pmc-standard weights. */
+/* An independent CPU run of a whole ABC-PMC estimation (abc_oracle.c),
+ * pmc-standard weights.  Models: lognormal diameters (model 2; parameters
+ * m | s | log10c | az, the depth fixed at az) or the reference's discrete
+ * diffusivities with one depth (model 0, discrete-fixed-depth; parameters
+ * m | log10c | az, the depth drawn from [lb_az, ub_az]).  Schedules: the
+ * q-quantile of the previous generation's distances (schedule 1), or the
+ * reference's (schedule 0): gamma_0 = the distance of rank N/2 of the prior
+ * pass, then gamma -= delta_gamma at the start of every generation.  With
+ * avg_trials > 0, a generation whose trials reach avg_trials x N is
+ * discarded and ends the run (converged). */
 typedef struct orc_abc_problem {
     uint32_t C, N, generations, kmin, V, R, B;
     double quantile;
@@ -201,9 +247,14 @@ typedef struct orc_abc_problem {
     double az, Lx, Ly, Lz, ax, ay, deltat, ub_de, temperature, viscosity;
     const uint32_t* frames;  /* [V] */
     const uint32_t* ref_sat; /* [R*B] */
+    uint32_t model, schedule, avg_trials, full_az_prior;
+    double delta_gamma, lb_az, ub_az;
 } orc_abc_problem;
+/* theta_out [N * P], w_out [N]; *generations_out (nullable) receives the
+ * generations committed after the prior pass and *converged_out (nullable)
+ * whether the trial cap ended the run.  Returns the total trials. */
 uint64_t orc_abc_pmc(const orc_abc_problem* pb, uint64_t seed, uint32_t nthreads, double* theta_out,
-                     double* w_out);
+                     double* w_out, uint32_t* generations_out, int* converged_out);
 
 #ifdef __cplusplus
 }

@@ -258,6 +258,20 @@ class Simulation:
         buf = C.create_string_buffer(bytes(data), len(data))
         check(lib().pcs_job_restore(self.h, buf, len(data)), "pcs_job_restore")
 
+    def round_proposals(self):
+        """This job's proposals in the context's last round: (list of
+        pcs_debug_proposal, theta [n, P], counts [n, V])."""
+        n = C.c_uint32(0)
+        check(lib().pcs_debug_round_proposals(self.h, 0, C.byref(n), None, None, None), "pcs_debug_round_proposals")
+        i = self.info()
+        P, V = i.param_count, len(self.input.frames)
+        props = (_lib.DebugProposal * max(1, n.value))()
+        theta = np.zeros((max(1, n.value), P))
+        counts = np.zeros((max(1, n.value), V), np.uint32)
+        check(lib().pcs_debug_round_proposals(self.h, n.value, C.byref(n), props, _p(theta, C.c_double),
+                                              _p(counts, C.c_uint32)), "pcs_debug_round_proposals")
+        return list(props)[:n.value], theta[:n.value], counts[:n.value]
+
     def close(self):
         if self.h:
             check(lib().pcs_job_destroy(self.h), "pcs_job_destroy")

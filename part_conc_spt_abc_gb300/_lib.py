@@ -108,6 +108,14 @@ class Replay(C.Structure):
     _fields_ = [("uniforms", _f32p), ("normals", _f32p), ("normal_stride", C.c_uint32), ("sigmas", _f32p)]
 
 
+class DebugProposal(C.Structure):
+    _fields_ = [
+        ("slot", C.c_uint32), ("trial", C.c_uint32), ("generation", C.c_uint32), ("total_particles", C.c_uint32),
+        ("half_az", C.c_float * MAX_COMPONENTS), ("pre_comp_prob", C.c_float * MAX_COMPONENTS),
+        ("sd_scale", C.c_float * MAX_COMPONENTS), ("sd_shape", C.c_float * MAX_COMPONENTS),
+    ]
+
+
 class OutputMeta(C.Structure):
     _fields_ = [("key", C.c_char_p), ("value", C.c_char_p)]
 
@@ -172,6 +180,7 @@ SIGNATURES = {
                                          _u32p]),
     "pcs_debug_particle_stream": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                             C.c_uint32, C.c_uint32, _u32p]),
+    "pcs_debug_round_proposals": (C.c_int, [C.c_void_p, C.c_uint32, _u32p, C.c_void_p, _f64p, _u32p]),
 }
 
 

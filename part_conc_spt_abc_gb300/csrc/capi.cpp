@@ -804,4 +804,54 @@ pcs_status pcs_debug_particle_stream(pcs_ctx* ctx, uint64_t seed, uint32_t slot,
     });
 }
 
+pcs_status pcs_debug_round_proposals(pcs_job* job, uint32_t cap, uint32_t* n, pcs_debug_proposal* props,
+                                     double* theta, uint32_t* counts)
+{
+    return guard([&] {
+        Job& j = J_(job);
+        need(n, "n");
+        Ctx& c = *j.ctx;
+        PCS_CUDA(cudaSetDevice(c.device));
+        if (j.slot < 0) throw Error(PCS_ERR_NOT_FOUND, "job is not in the round table (not admitted, or retired)");
+        if (!c.rb.round.p) throw Error(PCS_ERR_NOT_FOUND, "no round has run on this context");
+        PCS_CUDA(cudaStreamSynchronize(c.stream));
+        RoundDev rd;
+        PCS_CUDA(cudaMemcpy(&rd, c.rb.round.p, sizeof rd, cudaMemcpyDeviceToHost));
+        const uint32_t js = (uint32_t)j.slot;
+        const uint32_t cnt = js < rd.n_jobs ? rd.job_count[js] : 0u;
+        const uint32_t base = rd.job_base[js];
+        *n = cnt;
+        if (!props || cnt == 0) return;
+        if (cap < cnt) throw Error(PCS_ERR_INVALID_ARGUMENT, "cap is smaller than the round's proposals of the job");
+        need(theta, "theta");
+        need(counts, "counts");
+        std::vector<PropDev> pd(cnt);
+        std::vector<double> th((size_t)cnt * PCS_MAX_P);
+        const uint64_t stride = 2ull * rd.v_max + 1ull;
+        std::vector<uint32_t> cv((size_t)cnt * stride);
+        PCS_CUDA(cudaMemcpy(pd.data(), c.rb.props.as<PropDev>() + base, cnt * sizeof(PropDev), cudaMemcpyDeviceToHost));
+        PCS_CUDA(cudaMemcpy(th.data(), c.rb.theta_prop.as<double>() + (size_t)base * PCS_MAX_P, th.size() * 8,
+                            cudaMemcpyDeviceToHost));
+        PCS_CUDA(cudaMemcpy(cv.data(), c.rb.counts.as<uint32_t>() + base * stride, cv.size() * 4,
+                            cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i < cnt; ++i) {
+            const PropDev& q = pd[i];
+            pcs_debug_proposal& o = props[i];
+            o.slot = q.slot;
+            o.trial = q.trial;
+            o.generation = q.gen;
+            o.total_particles = q.total_particles;
+            for (int k = 0; k < PCS_MAX_COMPONENTS; ++k) {
+                o.half_az[k] = q.half_az[k];
+                o.pre_comp_prob[k] = q.pre_comp_prob[k];
+                o.sd_scale[k] = q.sd_scale[k];
+                o.sd_shape[k] = q.sd_shape[k];
+            }
+            for (uint32_t p = 0; p < j.P; ++p) theta[(size_t)i * j.P + p] = th[(size_t)i * PCS_MAX_P + p];
+            const uint64_t off = q.counts_off - (uint64_t)base * stride;
+            for (uint32_t v = 0; v < j.V; ++v) counts[(size_t)i * j.V + v] = cv[off + v];
+        }
+    });
+}
+
 } // extern "C"

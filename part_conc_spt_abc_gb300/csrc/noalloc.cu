@@ -22,12 +22,18 @@
  * The array's address is looked up once per device with cudaGetSymbolAddress
  * (the host-side name of a __device__ variable is only a stand-in): the first
  * call on a device does that lookup, so make the first call before any stream
- * capture.  Every call reuses the same array and overwrites what the previous
- * call left there; two calls whose work overlaps on the GPU (different
- * streams, not ordered) race on it and must not be issued.
+ * capture.  The address is kept for the life of the process, so the entry
+ * point does not survive cudaDeviceReset (or another release of the device's
+ * primary context), after which the array is reloaded at another address.
+ * Every call reuses the same array and overwrites what the previous call left
+ * there; two calls whose work overlaps on the GPU (different streams, not
+ * ordered) race on it and must not be issued.  Each call waits for its work
+ * on the caller's stream, reads the kernel's error word back and reports a
+ * raised word as PCS_ERR_DEVICE.
  */
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <mutex>
 #include <string>
 
@@ -165,5 +171,16 @@ extern "C" pcs_status pcs_scan_distance_noalloc(uint32_t* d_hist, const uint32_t
     const uint32_t grid = count < cap ? count : cap;
     e = pcs::launch_distance(d, grid ? grid : 1u, st);
     if (e != cudaSuccess) return fail_(PCS_ERR_CUDA, std::string("distance launch: ") + cudaGetErrorString(e));
+    /* wait for the work and read the kernel's error word back (a plain copy
+     * into this stack variable: the runtime stages pageable copies itself) */
+    uint32_t word = 0;
+    e = cudaMemcpyAsync(&word, &h->err, sizeof word, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail_(PCS_ERR_CUDA, std::string("distance kernel: ") + cudaGetErrorString(e));
+    if (word) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "distance kernel raised device error word 0x%x (32: histogram rows)", word);
+        return fail_(PCS_ERR_DEVICE, buf);
+    }
     return fail_(PCS_OK, "");
 }

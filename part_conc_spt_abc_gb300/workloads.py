@@ -96,6 +96,17 @@ def make_problem(ctx, mu, sd, conc_m3, weights, videos, frames, de_bins, pop, ge
     setup = forward_setup(fr, de_bins, C=C)
     run = lognormal_run(parts, mu, sd, np.asarray(weights) / np.sum(weights))
     hist = simulate_hist(ctx, setup, run, seed=seed)[0]
+    return problem_from_hist(hist, mu, sd, conc_m3, weights, videos, frames, pop, generations, prior_mu, prior_sd,
+                             prior_conc_m3, avg_trials, quantile)
+
+
+def problem_from_hist(hist, mu, sd, conc_m3, weights, videos, frames, pop, generations, prior_mu=(50.0, 1000.0),
+                      prior_sd=(1.0, 100.0), prior_conc_m3=(1e13, 1e15), avg_trials=500, quantile=0.5):
+    """Input for one lognormal estimation problem whose observed histogram
+    (R x B, DE over [0, UB_DE)) is given."""
+    C = len(mu)
+    de_bins = hist.shape[1]
+    fr = np.full(videos, frames, np.uint32)
     K, DE = observed_from_hist(hist, UB_DE)
     p = params_defaults()
     p.model = MODEL_LOGNORMAL

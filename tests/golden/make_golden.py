@@ -5,8 +5,8 @@ code, compiled for the host by oracle/build_ref.sh (oracle/_ref/libpcsref.so):
                      (src/gpu/cusim/kernel-simulate.inl) on replayed draws;
                      the draws are regenerated from the stored seed by
                      orc_replay_draws (oracle/pcs_oracle.h)
-  distance_cases.npz K_distance results of the oracle restatement
-                     (kernel-distance.inl:81-241) on seeded histograms
+  (distance_cases.npz comes from the reference's distance kernel run on a
+   GPU: make_distance_golden.py)
   xml_cases.json     input::load (src/gpu/shared/input.cpp) on the XML files
                      in tests/golden/xml/: parsed values or the error type
   output_cases.json  output::write (src/gpu/shared/output.cpp) bytes for
@@ -99,28 +99,6 @@ def replay_cases():
     print("replay cases:", len(cases))
 
 
-def distance_cases():
-    rng = np.random.default_rng(99)
-    out = {}
-    shapes = [(201, 100), (37, 5), (301, 128), (33, 64), (1, 1), (65, 33), (1001, 40)]
-    for i, (R, B) in enumerate(shapes):
-        hist = rng.poisson(rng.uniform(0.0, 3.0), (R, B)).astype(np.uint32)
-        hist[0, :] = 0
-        obs = rng.poisson(1.5, (R, B)).astype(np.uint32)
-        ref = np.cumsum(np.cumsum(obs.astype(np.uint64), 0), 1).astype(np.uint32)
-        d, cum, ssd = O.distance_kdist(hist, ref)
-        d64 = O.distance_kdist_f64(hist, ref)
-        out[f"c{i}_hist"] = hist
-        out[f"c{i}_ref"] = ref
-        out[f"c{i}_cum"] = cum
-        out[f"c{i}_dist"] = np.array([d], np.float32)
-        out[f"c{i}_dist64"] = np.array([d64], np.float64)
-        out[f"c{i}_ssd"] = np.array([ssd >> 64, ssd & ((1 << 64) - 1)], np.uint64)
-    out["count"] = np.array([len(shapes)])
-    np.savez_compressed(os.path.join(HERE, "distance_cases.npz"), **out)
-    print("distance cases:", len(shapes))
-
-
 # ---------------------------------------------------------------- XML ------
 
 class RefParams(C.Structure):
@@ -177,9 +155,9 @@ def xml_cases():
             continue
         res[name] = {"data": os.path.basename(data), "ref": ref_input_load(inp, data)}
     # the reference's own fixture (test_files/), when the tree is present
-    ref_root = os.environ.get("PCS_REFERENCE_ROOT", "/root/reference")
-    tf = os.path.join(ref_root, "test_files")
-    if os.path.isdir(tf):
+    ref_root = O.reference_root()
+    tf = os.path.join(ref_root, "test_files") if ref_root else ""
+    if tf and os.path.isdir(tf):
         res["test_files/input.xml"] = {"data": "test_files/data_20171018_175nm_500nm.xml",
                                        "ref": ref_input_load(os.path.join(tf, "input.xml"),
                                                              os.path.join(tf, "data_20171018_175nm_500nm.xml"))}
@@ -227,6 +205,5 @@ if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("oracle/_ref/libpcsref.so is missing: the reference tree is needed to make the fixtures")
     replay_cases()
-    distance_cases()
     xml_cases()
     output_cases()

@@ -6,6 +6,7 @@ in the reference reduction order, exact sums of squares, observed cumulative
 histograms, raw Philox words.  Statistical: histograms on the product's own
 random streams against the oracle on the same streams."""
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -47,16 +48,42 @@ def test_replay_lognormal_bit_exact(pcs, ctx, oracle):
     assert want.sum() > 0 and np.array_equal(got, want)
 
 
-def test_distance_golden_bit_exact(pcs, ctx):
-    zf = np.load(os.path.join(GOLDEN, "distance_cases.npz"))
-    for i in range(int(zf["count"][0])):
-        h, ref = zf[f"c{i}_hist"], zf[f"c{i}_ref"]
+def _distance_cases():
+    sys.path.insert(0, GOLDEN)
+    import distance_inputs as D
+    return D, np.load(os.path.join(GOLDEN, "distance_cases.npz"))
+
+
+def test_distance_golden_bit_exact(pcs, ctx, oracle):
+    """Against the reference's own K_distance (kernel-distance.inl:81-241)
+    built without FMA contraction and run on a GPU: float and double
+    distances bit for bit; prefix sums and the exact integer sum of squares
+    against numpy and the oracle."""
+    D, zf = _distance_cases()
+    for i, case in enumerate(D.CASES):
+        h, ref = D.case_arrays(case)
         r = pcs.scan_distance(ctx, h, ref, want_cum=True, want_f64=True, want_ssd=True)
-        assert r["dist_f32"][0].tobytes() == zf[f"c{i}_dist"][0].tobytes(), i
-        assert r["dist_f64"][0] == zf[f"c{i}_dist64"][0], i
-        assert np.array_equal(r["cum"][0], zf[f"c{i}_cum"]), i
-        hi, lo = zf[f"c{i}_ssd"]
-        assert r["ssd"][0] == (int(hi) << 64) | int(lo), i
+        assert r["dist_f32"][0].tobytes() == zf[f"c{i}_ref_f32_nofma"][0].tobytes(), case[0]
+        assert r["dist_f64"][0] == zf[f"c{i}_ref_f64_nofma"][0], case[0]
+        assert np.array_equal(r["cum"][0], D.sat(h)), case[0]
+        assert r["ssd"][0] == oracle.distance_kdist(h, ref)[2], case[0]
+        # the PMC rounds' variant (float sum only) gives the same float
+        assert pcs.scan_distance(ctx, h, ref)["dist_f32"][0] == r["dist_f32"][0], case[0]
+
+
+def test_distance_within_bound_of_shipped_reference(pcs, ctx):
+    """The reference as it ships is compiled with nvcc's default FMA
+    contraction (premake5.lua:76), which fuses `a2 += dd*dd`; this library
+    keeps every product and sum a separate rounding.  The two differ at most
+    by the float-summation bound of distance_inputs.fma_bound."""
+    D, zf = _distance_cases()
+    for i, case in enumerate(D.CASES):
+        name, R, B = case[:3]
+        h, ref = D.case_arrays(case)
+        r = pcs.scan_distance(ctx, h, ref, want_f64=True)
+        for got, key, bits in ((float(r["dist_f32"][0]), "f32", 24), (float(r["dist_f64"][0]), "f64", 53)):
+            want = float(zf[f"c{i}_ref_{key}_fma"][0])
+            assert abs(got - want) <= D.fma_bound(R, B, want, bits), (name, key, got, want)
 
 
 @pytest.mark.parametrize("want_f64,want_ssd", [(False, True), (False, False), (True, False), (True, True)])

@@ -50,16 +50,45 @@ def test_replay_matches_reference_kernel_random(oracle):
 
 
 def test_distance_golden(oracle):
+    """The oracle's K_distance restatement against the reference's own
+    kernel (kernel-distance.inl:81-241) built without FMA contraction and run
+    on a GPU (tests/golden/make_distance_golden.py): float and double sums
+    bit for bit, on every case of distance_inputs.py."""
     import os
+    import sys
     from conftest import GOLDEN
+    sys.path.insert(0, GOLDEN)
+    import distance_inputs as D
     z = np.load(os.path.join(GOLDEN, "distance_cases.npz"))
-    for i in range(int(z["count"][0])):
-        d, cum, ssd = oracle.distance_kdist(z[f"c{i}_hist"], z[f"c{i}_ref"])
-        assert np.float32(d).tobytes() == z[f"c{i}_dist"][0].tobytes()
-        assert np.array_equal(cum, z[f"c{i}_cum"])
-        hi, lo = z[f"c{i}_ssd"]
-        assert ssd == (int(hi) << 64) | int(lo)
-        assert oracle.distance_kdist_f64(z[f"c{i}_hist"], z[f"c{i}_ref"]) == z[f"c{i}_dist64"][0]
+    assert int(z["count"][0]) == len(D.CASES)
+    for i, case in enumerate(D.CASES):
+        assert str(z[f"c{i}_name"]) == case[0]
+        hist, ref = D.case_arrays(case)
+        d, cum, ssd = oracle.distance_kdist(hist, ref)
+        assert np.float32(d).tobytes() == z[f"c{i}_ref_f32_nofma"][0].tobytes(), case[0]
+        assert oracle.distance_kdist_f64(hist, ref) == z[f"c{i}_ref_f64_nofma"][0], case[0]
+        assert int(z[f"c{i}_zeroed"][0]) == 1, "the reference kernel resets the histogram"
+        assert np.array_equal(cum, D.sat(hist))
+        diff = cum.astype(np.int64) - ref.astype(np.int64)
+        assert ssd == int(np.sum(diff.astype(object) ** 2)), case[0]
+
+
+def test_distance_fma_build_within_bound(oracle):
+    """The reference as shipped (nvcc's default FMA contraction) differs from
+    the contraction-free contract only within the float-summation bound."""
+    import os
+    import sys
+    from conftest import GOLDEN
+    sys.path.insert(0, GOLDEN)
+    import distance_inputs as D
+    z = np.load(os.path.join(GOLDEN, "distance_cases.npz"))
+    differs = 0
+    for i, (name, R, B, *_rest) in enumerate(D.CASES):
+        for bits, key in ((24, "f32"), (53, "f64")):
+            a, b = float(z[f"c{i}_ref_{key}_nofma"][0]), float(z[f"c{i}_ref_{key}_fma"][0])
+            assert abs(a - b) <= D.fma_bound(R, B, a, bits), (name, key, a, b)
+            differs += a != b
+    assert differs > 0, "the two builds are expected to differ somewhere"
 
 
 def test_distance_properties(oracle):
@@ -164,3 +193,48 @@ def test_split_walk_has_the_per_step_distribution(oracle, mu, F):
     se = np.sqrt(a.var(0, ddof=1) / reps + b.var(0, ddof=1) / reps)
     z = np.abs(a.mean(0) - b.mean(0)) / se
     assert (z < 4.0).all(), (a.mean(0), b.mean(0), z)
+
+
+def test_oracle_proposal_against_its_distributions(oracle):
+    """orc_build_proposal on many (slot, trial) streams: parents drawn in
+    proportion to the weights (chi-square), every parameter in its prior box,
+    components sorted by m, Poisson counts with the right mean and variance
+    for a mean below 12 (inversion) and above (PTRS), and the prior pass
+    taking the slot's own parameters."""
+    from types import SimpleNamespace
+    rng = np.random.default_rng(3)
+    N, Cc = 40, 2
+    par = SimpleNamespace(component_count=Cc, model=oracle.MODEL_LOGNORMAL, abc_sample_count=N, perturbation=0,
+                          reference_initial_gamma=0, Lx=200.0, Ly=160.0, Lz=20.0, lb_m=50.0, ub_m=1000.0, lb_s=1.0,
+                          ub_s=100.0, lb_c=1e7, ub_c=1e9, lb_az=2.0, ub_az=2.0, temperature=298.0,
+                          viscosity=0.95e-3)
+    job = oracle.prop_job(par, 16, 1 / 30, 77)
+    P = job.P
+    lo, hi = np.array(job.lo[:P]), np.array(job.hi[:P])
+    theta = lo + (hi - lo) * rng.uniform(size=(N, P))
+    w = rng.uniform(0.2, 1.0, N)
+    w /= w.sum()
+    wcum = np.cumsum(w)
+    factor = np.diag(0.3 * (hi - lo))
+    parents = np.zeros(N)
+    for t in range(4000):
+        th, cn, op = oracle.build_proposal(job, theta, wcum, factor, t % N, t // N, 3)
+        parents[op.parent] += 1
+        assert (th >= lo).all() and (th <= hi).all()
+        assert th[0] <= th[1], "components sorted by m"
+        assert op.total_particles == cn.sum()
+    chi2 = ((parents - 4000 * w) ** 2 / (4000 * w)).sum()
+    assert chi2 < 80, chi2  # 39 degrees of freedom: p ~ 1e-4
+    for lc in (np.log10(3e7), np.log10(8e8)):  # lambda ~ 5.8 and ~ 154 per video
+        th0 = theta.copy()
+        th0[:, 4:6] = lc - np.log10(2.0)  # two components of half the concentration each
+        cs = []
+        for s in range(N):
+            th, cn, op = oracle.build_proposal(job, th0, wcum, factor, s, 0, 0)
+            assert np.array_equal(th, th0[s]), "the prior pass simulates the slot's own parameters"
+            cs.append(cn)
+        cs = np.concatenate(cs).astype(float)
+        lam = op.lambda_
+        se = np.sqrt(lam / cs.size)
+        assert abs(cs.mean() - lam) < 4 * se, (lam, cs.mean())
+        assert abs(cs.var() / lam - 1) < 0.15, (lam, cs.var())

@@ -7,16 +7,25 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, ROOT
 
 XML = os.path.join(GOLDEN, "xml")
 CASES = json.load(open(os.path.join(GOLDEN, "xml_cases.json")))
-REF_ROOT = os.environ.get("PCS_REFERENCE_ROOT", "/root/reference")
+
+
+def _reference_root():
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    return oracle.reference_root()
 
 
 def _paths(name, case):
     if name.startswith("test_files/"):
-        return os.path.join(REF_ROOT, name), os.path.join(REF_ROOT, case["data"])
+        root = _reference_root()
+        if root is None:
+            return "", ""
+        return os.path.join(root, name), os.path.join(root, case["data"])
     return os.path.join(XML, name), os.path.join(XML, case["data"])
 
 
