@@ -5,8 +5,17 @@ Workload (configuration 1): two-component lognormal mixture
 (175/500 nm, sd 10/25 nm, weights 0.6/0.4, 5e14 m^-3), 50 videos x 300
 frames, population 1024, epsilon = 50% quantile, histograms 301 x 128.  A
 step is one ABC-PMC generation (batched rounds until every population slot
-has accepted a proposal).  The metric is particle-steps/s (one walk step of
-one particle; initial placements count as steps), whole job, all GPUs.
+has accepted a proposal) of a sequence of such jobs run back to back, each
+capped at the configuration's 12 generations.  The metric is
+particle-steps/s (one walk step of one particle; initial placements count
+as steps), whole job, all GPUs.
+
+At N = 1 the line also carries, as extra keys, short runs of
+configurations 2 (512-proposal rounds) and 3 (a 64-proposal slice of the
+1e5-particles-per-video model), the PMC step's time at population 4096, and
+`serve`: the 64-job serving stream (p50/p99 job latency, accepted
+proposals/s) and the served / plain ratio of accepted proposals/s on equal
+work, each with its own clock record (--headline-only leaves them out).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -262,31 +271,27 @@ def plain_stream_run(P, ctx, jobs, arrivals, budget_s, geometry):
             "particle_steps_per_s": steps / max(clock, 1e-9)}
 
 
-def run_serve(args, rank, world):
-    """The serving stream (configuration 4): jobs arrive as a
-    Poisson process at 2 jobs/s.  The served form admits them into the
-    continuous-batching loop as they arrive (headline: p50/p99 latency and
-    accepted proposals/s over the whole stream).  The plain form runs jobs
-    one at a time in arrival order with the reference's per-proposal
-    schedule; it cannot finish the stream in minutes, so the served/plain
-    ratio is taken on equal work at saturation: the first --cmp-jobs jobs of
-    the stream, each capped at --cmp-generations generations after the prior
-    pass, all submitted at time 0, run by the plain form (one job after
-    another; reference launch geometry, and the library's persistent grid)
-    and by the served form (all jobs at once)."""
-    import part_conc_spt_abc_gb300 as P
+def serve_section(args, P, device: int):
+    """The serving stream (configuration 4): jobs arrive as a Poisson
+    process at 2 jobs/s.  The served form admits them into the
+    continuous-batching loop as they arrive (p50/p99 latency and accepted
+    proposals/s over the whole stream).  The plain form runs jobs one at a
+    time with the reference's per-proposal schedule; it cannot finish the
+    stream in minutes, so the served/plain ratio is taken on equal work at
+    saturation: the first --cmp-jobs jobs of the stream, each capped at
+    --cmp-generations generations after the prior pass, all submitted at
+    time 0, run by the plain form (one job after another; the reference's
+    launch geometry, and the library's persistent grid) and by the served
+    form (all jobs at once).  Clocks are sampled throughout."""
     import part_conc_spt_abc_gb300.workloads as W
-    ctx = P.Context(rank)
+    ctx = P.Context(device)
     if args.job_order:
         ctx.set_tuning(job_order=args.job_order)
+    ctx.set_tuning(walk=1 if args.walk == "split" else 2)
     jobs, arrivals = W.serve_stream(ctx, n_jobs=args.jobs, seed=args.seed)
+    clocks = Clocks(device)
+    t0 = time.perf_counter()
     res = {"served": serve_stream_run(P, ctx, jobs, arrivals), "job_order": ctx.tuning.job_order}
-    if args.cmp_jobs == 0:
-        line = {"metric": "serve p50/p99 job latency, accepted proposals/s", "value": res["served"]["accepted_per_s"],
-                "unit": "accepted proposals/s", "n_gpus": 1, **res}
-        print(json.dumps(line), flush=True)
-        ctx.close()
-        return
     cmp_jobs = []
     for inp, truth, seed in jobs[:args.cmp_jobs]:
         inp.params.max_generations = args.cmp_generations
@@ -294,6 +299,8 @@ def run_serve(args, rank, world):
     cmp_arr = np.zeros(len(cmp_jobs))
     comparisons = {}
     for name, geometry in (("reference_launch", 1), ("persistent_grid", 2)):
+        if not cmp_jobs:
+            break
         plain = plain_stream_run(P, ctx, cmp_jobs, cmp_arr, args.plain_budget, geometry)
         J = plain["jobs"]
         if J == 0:
@@ -304,18 +311,51 @@ def run_serve(args, rank, world):
                              "served_over_plain_accepted_per_s":
                                  served_j["accepted_per_s"] / max(plain["accepted_per_s"], 1e-12)}
     res["equal_work"] = comparisons
-    line = {"metric": "serve p50/p99 job latency, accepted proposals/s (served vs plain)",
-            "value": res["served"]["accepted_per_s"], "unit": "accepted proposals/s", "n_gpus": 1,
-            "config": {"workload": f"serving stream: {len(jobs)} jobs, Poisson arrivals 2/s, 1-3 lognormal "
-                                   "components, 100-500 frames, 64-256 DE bins, pop 256-4096, 6-12 generations",
-                       "equal_work": f"first {len(cmp_jobs)} jobs, {args.cmp_generations} generations after the "
-                                     f"prior pass each, all submitted at time 0, plain budget "
-                                     f"{args.plain_budget:.0f} s per form",
-                       "plain_forms": "reference_launch: ceil(V/4) CTAs x 128 threads per proposal, as the "
-                                      "reference launches its kernel; persistent_grid: the library's persistent grid"},
-            **res}
-    print(json.dumps(line), flush=True)
+    res["wall_s"] = time.perf_counter() - t0
+    res["clocks"] = clocks.stop()
+    res["config"] = {
+        "workload": f"serving stream: {len(jobs)} jobs, Poisson arrivals 2/s, 1-3 lognormal components, 100-500 "
+                    "frames, 64-256 DE bins, pop 256-4096, 6-12 generations",
+        "equal_work": f"first {len(cmp_jobs)} jobs, {args.cmp_generations} generations after the prior pass "
+                      f"each, all submitted at time 0, plain budget {args.plain_budget:.0f} s per form",
+        "plain_forms": "reference_launch: ceil(V/4) CTAs x 128 threads per proposal, as the reference launches "
+                       "its kernel; persistent_grid: the library's persistent grid"}
     ctx.close()
+    return res
+
+
+def pmc_at_pop4096(P, device: int):
+    """The PMC step (accept, whiten, pairwise kernel sum, finalize) at
+    population 4096, the largest of configuration 3 and the serving stream:
+    a configuration-0-shaped job with N = 4096, its prior pass and two
+    generations.  Reports the PMC step's CUDA-event span per ended
+    generation next to the generations' whole GPU time."""
+    import part_conc_spt_abc_gb300.workloads as W
+    ctx = P.Context(device)
+    inp, _ = W.make_problem(ctx, [175.0], [10.0], 2e14, [1.0], 20, 200, 100, 4096, 2, seed=0)
+    sim = P.make_simulation(ctx, inp, 1)
+    ctx.reset_kernel_stats()
+    for _ in range(3):
+        if sim.step():
+            break
+    ks = ctx.kernel_stats()
+    sim.close()
+    ctx.close()
+    g = max(1, ks.generations)
+    return {"population": 4096, "generations_ended": int(ks.generations), "rounds": int(ks.rounds),
+            "pmc_ms_per_generation": ks.pmc_ms / g, "gpu_ms_per_generation": ks.round_ms / g,
+            "pmc_share": ks.pmc_ms / max(ks.round_ms, 1e-9),
+            "pair_tflops": ks.pmc_pair_flops / max(ks.pmc_ms, 1e-9) / 1e9,
+            "workload": "configuration 0 shape (20 videos x 200 frames, 201 x 100 bins) with population 4096"}
+
+
+def run_serve(args, rank, world):
+    """--serve: the serving stream alone, as its own line."""
+    import part_conc_spt_abc_gb300 as P
+    res = serve_section(args, P, rank)
+    line = {"metric": "serve p50/p99 job latency, accepted proposals/s (served vs plain)",
+            "value": res["served"]["accepted_per_s"], "unit": "accepted proposals/s", "n_gpus": 1, **res}
+    print(json.dumps(line), flush=True)
 
 
 class JobSequence:
@@ -397,69 +437,59 @@ def run_plain_config(args, P, ctx, inp, workload, rank):
     ctx.close()
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--small", action="store_true", help="configuration 0 (pop 256): the case profiled under ncu")
-    ap.add_argument("--plain", type=int, default=0, choices=[0, 1, 2],
-                    help="time the plain form instead (1: reference launch geometry, 2: persistent grid) "
-                         "over --steps generations")
-    ap.add_argument("--walk", default="step", choices=["step", "split"],
-                    help="forward-model walk on Philox streams: per step (default) or slab-split")
-    ap.add_argument("--no-round-fill", action="store_true",
-                    help="no extra trials for rounds that would underfill the GPU")
-    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3],
-                    help="benchmark configuration (1 is the headline; 3 times a fixed 64-proposal slice)")
-    ap.add_argument("--serve", action="store_true", help="the 64-job serving stream, served vs plain")
-    ap.add_argument("--jobs", type=int, default=64)
-    ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--plain-budget", type=float, default=300.0, help="seconds allowed for each plain form")
-    ap.add_argument("--job-order", type=int, default=0, choices=[0, 1, 2],
-                    help="serve: capacity order among jobs (1 admission, 2 least remaining work; 0 library default)")
-    ap.add_argument("--cmp-jobs", type=int, default=4, help="serve: jobs in the equal-work comparison")
-    ap.add_argument("--cmp-generations", type=int, default=6, help="serve: generations per compared job")
-    args = ap.parse_args()
-    if args.warmup < 3:
-        ap.error("--warmup must be >= 3")
-    rank, world, local = dist_setup()
-    if args.impl == "reference":
-        run_reference(args, rank, world)
-        return
-    if args.serve:
-        run_serve(args, local, world)
-        return
-
-    import part_conc_spt_abc_gb300 as P
+def config_input(P, ctx, cfg, args):
+    """(input, workload text, step text) of configuration cfg on ctx, with the
+    context tuned for it (walk, autotuner, round capacity)."""
     import part_conc_spt_abc_gb300.workloads as W
-
-    peaks, peak_src = measured_peaks()
-    ctx = P.Context(local)
-    cfg = 0 if args.small else args.config
     workload, step_def = WORKLOADS[cfg]
-    gens = GENERATIONS[cfg]
-    inp, truth = {0: W.config0, 1: W.config1, 2: W.config2, 3: W.config3}[cfg](ctx, seed=0, generations=gens)
+    inp, _ = {0: W.config0, 1: W.config1, 2: W.config2, 3: W.config3}[cfg](ctx, seed=0, generations=GENERATIONS[cfg])
+    ctx.set_tuning(walk=1 if args.walk == "split" else 2)
     if not args.no_autotune and cfg != 3:
         ctx.autotune(inp)
-    ctx.set_tuning(walk=1 if args.walk == "split" else 2)
     if args.no_round_fill:
         ctx.set_tuning(round_fill=0xFFFFFFFF)
     if cfg == 2:
         ctx.set_tuning(round_capacity=512)
     if cfg == 3:
         ctx.set_tuning(round_capacity=64)
+    return inp, workload, step_def
+
+
+def e2e_run(P, ctx, inp, sequence, steps, rank, world):
+    """The same steps end to end through the public API from host buffers:
+    job creation (H2D of the observed data) inside the timing, the
+    population read back after every step (D2H)."""
+    barrier(world)
+    t0 = time.perf_counter()
+    seq2 = sequence(501 + 1000 * rank, 0)
+    d2h_total = 0
+    for _ in range(steps):
+        sim2 = seq2.step()
+        out = sim2.output()  # D2H: the population (m, s, c, az, dist, w)
+        d2h_total += sum(a.nbytes for a in (out.m, out.c, out.az, out.dist, out.w, out.s) if a is not None)
+    e2e_s = time.perf_counter() - t0
+    e2e_steps = seq2.totals()[0]
+    e2e_jobs = len(seq2.sims)
+    seq2.close()
+    e2e_s = allreduce(e2e_s, "max", world)
+    e2e_value = allreduce(float(e2e_steps), "sum", world) / e2e_s
+    h2d = e2e_jobs * (inp.K.nbytes + inp.DE.nbytes + inp.frames.nbytes) / steps
+    d2h = d2h_total / steps
+
+    return e2e_value, h2d, d2h
+
+
+def measure_config(args, P, cfg, steps, warmup, rank, world, local, e2e=True):
+    """One configuration's bench line: `steps` timed steps after `warmup`,
+    on a fresh context (its own tuning)."""
+    peaks, peak_src = measured_peaks()
+    ctx = P.Context(local)
+    inp, workload, step_def = config_input(P, ctx, cfg, args)
     t = ctx.tuning
-    tune = dict(walk={1: "slab-split", 2: "per-step"}.get(t.walk, t.walk), round_fill=t.round_fill, block=t.block_size, ppt=t.particles_per_thread, tile_rows=t.hist_tile_rows,
+    tune = dict(walk={1: "slab-split", 2: "per-step"}.get(t.walk, t.walk), round_fill=t.round_fill,
+                block=t.block_size, ppt=t.particles_per_thread, tile_rows=t.hist_tile_rows,
                 warp_aggregate=t.warp_aggregate, chunk=t.chunk_particles, capacity=t.round_capacity,
                 autotuned=not args.no_autotune and cfg != 3)
-
-    if args.plain:
-        run_plain_config(args, P, ctx, inp, workload, rank)
-        return
 
     class SliceSteps:
         """configuration 3: one round of the fixed 64-proposal prior-pass slice per step"""
@@ -488,8 +518,8 @@ def main():
     # ---- device-resident run: inputs already in HBM -----------------------
     # every job the warm-up and the timed steps can need is created (its
     # observed data uploaded) before the timed region
-    seq = sequence(1 + 1000 * rank, args.warmup + args.steps)
-    for _ in range(args.warmup):
+    seq = sequence(1 + 1000 * rank, warmup + steps)
+    for _ in range(warmup):
         seq.step()
     barrier(world)
     ctx.reset_kernel_stats()
@@ -497,7 +527,7 @@ def main():
     jobs0 = seq.jobs_finished
     clocks = Clocks(local)
     ctx.timer_start()
-    for _ in range(args.steps):
+    for _ in range(steps):
         seq.step()
     ms = ctx.timer_stop()
     clk = clocks.stop()
@@ -517,22 +547,9 @@ def main():
     # ---- end to end through the public API, host buffers ------------------
     # jobs are created inside the timed region here (H2D: observed K, DE,
     # frame counts); each step reads the population back (D2H)
-    barrier(world)
-    t0 = time.perf_counter()
-    seq2 = sequence(501 + 1000 * rank, 0)
-    d2h_total = 0
-    for _ in range(args.steps):
-        sim2 = seq2.step()
-        out = sim2.output()  # D2H: the population (m, s, c, az, dist, w)
-        d2h_total += sum(a.nbytes for a in (out.m, out.c, out.az, out.dist, out.w, out.s) if a is not None)
-    e2e_s = time.perf_counter() - t0
-    e2e_steps = seq2.totals()[0]
-    e2e_jobs = len(seq2.sims)
-    seq2.close()
-    e2e_s = allreduce(e2e_s, "max", world)
-    e2e_value = allreduce(float(e2e_steps), "sum", world) / e2e_s
-    h2d = e2e_jobs * (inp.K.nbytes + inp.DE.nbytes + inp.frames.nbytes) / args.steps
-    d2h = d2h_total / args.steps
+    e2e_value, h2d, d2h = None, 0, 0
+    if e2e:
+        e2e_value, h2d, d2h = e2e_run(P, ctx, inp, sequence, steps, rank, world)
 
     # ---- roofline of the dominant kernel (forward model: issue bound) -----
     sim_ms = ks.simulate_ms / max(1, ks.simulate_launches)
@@ -557,16 +574,16 @@ def main():
                + (" (above L2)" if cells * 4 > 129e6 else " (below L2; the kernels are issue-bound)"))
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms_max / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload, "step": step_def, "parallelism": f"replicas x{world}",
                    "l2": l2_note, "tuning": tune,
-                   "timed_region": {"steps": args.steps, "generations_ended": int(ks.generations),
+                   "timed_region": {"steps": steps, "generations_ended": int(ks.generations),
                                     "jobs_ended": jobs_ended, "generation_cap": GENERATIONS[cfg]}},
         "proposals_per_s": props_all / (ms_max / 1e3),
         "accepted_per_s": acc_all / (ms_max / 1e3),
-        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+        "e2e": ({"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
+                 "d2h_bytes_per_step": int(d2h)} if e2e else None),
         "gpu_launches": int(ks.kernel_launches),
         "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tops/s",
                      "frac": achieved / peak, "traffic": traffic,
@@ -591,8 +608,73 @@ def main():
                       "rounds": int(ks.rounds), "round_ms_total": ks.round_ms},
         "clocks": clk,
     }
+    ctx.close()
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="configuration 0 (pop 256): the case profiled under ncu")
+    ap.add_argument("--plain", type=int, default=0, choices=[0, 1, 2],
+                    help="time the plain form instead (1: reference launch geometry, 2: persistent grid) "
+                         "over --steps generations")
+    ap.add_argument("--walk", default="step", choices=["step", "split"],
+                    help="forward-model walk on Philox streams: per step (default) or slab-split")
+    ap.add_argument("--no-round-fill", action="store_true",
+                    help="no extra trials for rounds that would underfill the GPU")
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3],
+                    help="benchmark configuration (1 is the headline; 3 times a fixed 64-proposal slice)")
+    ap.add_argument("--serve", action="store_true", help="the 64-job serving stream, served vs plain")
+    ap.add_argument("--jobs", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--plain-budget", type=float, default=300.0, help="seconds allowed for each plain form")
+    ap.add_argument("--job-order", type=int, default=0, choices=[0, 1, 2],
+                    help="serve: capacity order among jobs (1 admission, 2 least remaining work; 0 library default)")
+    ap.add_argument("--cmp-jobs", type=int, default=4, help="serve: jobs in the equal-work comparison")
+    ap.add_argument("--cmp-generations", type=int, default=6, help="serve: generations per compared job")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="configuration 1 alone: no configuration 2 / 3 slices, PMC timing or serving stream")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if args.serve:
+        run_serve(args, local, world)
+        return
+
+    import part_conc_spt_abc_gb300 as P
+
+    cfg = 0 if args.small else args.config
+    if args.plain:
+        ctx = P.Context(local)
+        inp, workload, _ = config_input(P, ctx, cfg, args)
+        run_plain_config(args, P, ctx, inp, workload, rank)
+        return
+    line = measure_config(args, P, cfg, args.steps, args.warmup, rank, world, local, e2e=True)
     if cfg != 1:
         line["config"]["headline"] = False
+    if cfg == 1 and world == 1 and not args.headline_only:
+        # other configurations as extra keys: short runs, not the headline
+        for extra in (2, 3):
+            x = measure_config(args, P, extra, 3, 3, rank, world, local, e2e=False)
+            line[f"config{extra}"] = {k: x[k] for k in ("value", "unit", "steps", "ms_per_step", "proposals_per_s",
+                                                          "accepted_per_s", "roofline", "roofline_distance",
+                                                          "kernel_ms", "clocks") if k in x}
+            line[f"config{extra}"]["workload"] = x["config"]["workload"]
+            line[f"config{extra}"]["step"] = x["config"]["step"]
+            line[f"config{extra}"]["tuning"] = x["config"]["tuning"]
+        line["pmc_pop4096"] = pmc_at_pop4096(P, local)
+        # the serving stream and the served / plain comparison (spec target)
+        line["serve"] = serve_section(args, P, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline and cfg == 1:
         threads = os.cpu_count() or 1
         sample, n = cpu_port_sample(10.0, threads)
@@ -601,7 +683,6 @@ def main():
                                 "sample": f"{n} config-1 forward simulations (Julia conventions, Float64), {s:.1f} s"}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     barrier(world)
 
 

@@ -138,7 +138,8 @@ size_t pcs_device_report(char* buf, size_t cap);
 #define PCS_TUNE_ZERO 0xFFFFFFFFu
 typedef struct pcs_tuning {
     uint32_t block_size;          /* forward-model threads per CTA */
-    uint32_t particles_per_thread;/* independent walkers interleaved per thread: 1, 2 or 4 */
+    uint32_t particles_per_thread;/* independent walkers interleaved per thread: 1, 2, 4 or 8;
+                                   * block_size is then at most 1024, 512, 256 or 256 */
     uint32_t hist_tile_rows;      /* histogram rows privatised in shared memory.  0 (default):
                                    * none; records are global atomics and each warp takes its
                                    * own 32-particle slices of the work items (no CTA barrier) */

@@ -4,7 +4,8 @@
  * Times the fused simulate kernel on the first batched round of a job of
  * the requested shape (its prior-pass proposals: real Poisson particle
  * counts, real frame counts) over a grid of block sizes (128-1024),
- * interleaved walkers per thread (1, 2, 4), shared-memory histogram tiles
+ * interleaved walkers per thread (1, 2, 4, 8; each count's build limits
+ * its block size, sim_max_block), shared-memory histogram tiles
  * and warp aggregation, and keeps the fastest.  The reference has no
  * counterpart; its launch shape is fixed at ceil(V/4) x 128
  * (src/gpu/detail/simulation_impl.inl:655-656).
@@ -93,7 +94,7 @@ void autotune(Ctx& c, const pcs_params& p, const pcs_observed& obs, pcs_tuning* 
         const uint32_t B = std::max<uint32_t>(c.rb_max_b_, 1u);
         std::vector<Candidate> grid;
         const uint32_t blocks[] = {128, 256, 512, 1024};
-        const uint32_t ppts[] = {1, 2, 4};
+        const uint32_t ppts[] = {1, 2, 4, 8};
         const uint32_t tiles[] = {0, 32, 64, 128, 256};
         for (uint32_t b : blocks)
             for (uint32_t pp : ppts)
@@ -101,6 +102,7 @@ void autotune(Ctx& c, const pcs_params& p, const pcs_observed& obs, pcs_tuning* 
                     for (uint32_t g = 0; g < 2; ++g) {
                         if (t == 0 && g == 1) continue;
                         if ((size_t)t * B * 4u > 200u * 1024u) continue;
+                        if (b > sim_max_block((int)pp)) continue; /* above the build's launch bound */
                         if (t > job.R) continue;
                         if (c.split_walk() && (pp != 1u || b != 256u)) continue; /* fixed shape */
                         SimLaunch l{0, b, (int)pp, false, g != 0, c.split_walk()};

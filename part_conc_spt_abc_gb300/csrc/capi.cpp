@@ -221,10 +221,16 @@ pcs_status pcs_set_tuning(pcs_ctx* ctx, const pcs_tuning* t)
             c.tune.block = t->block_size;
         }
         if (t->particles_per_thread) {
-            if (t->particles_per_thread != 1 && t->particles_per_thread != 2 && t->particles_per_thread != 4)
-                throw Error(PCS_ERR_INVALID_ARGUMENT, "particles_per_thread must be 1, 2 or 4");
-            c.tune.ppt = t->particles_per_thread;
+            const uint32_t pp = t->particles_per_thread;
+            if (pp != 1 && pp != 2 && pp != 4 && pp != 8)
+                throw Error(PCS_ERR_INVALID_ARGUMENT, "particles_per_thread must be 1, 2, 4 or 8");
+            c.tune.ppt = pp;
         }
+        if (c.tune.block > sim_max_block((int)c.tune.ppt))
+            throw Error(PCS_ERR_INVALID_ARGUMENT,
+                        "block_size " + std::to_string(c.tune.block) + " is above the " +
+                            std::to_string(sim_max_block((int)c.tune.ppt)) + " threads of the build for " +
+                            std::to_string(c.tune.ppt) + " walkers per thread");
         if (t->hist_tile_rows) c.tune.tile_rows = t->hist_tile_rows == 0xFFFFFFFFu ? 0u : t->hist_tile_rows;
         if (t->warp_aggregate) c.tune.aggregate = t->warp_aggregate == 1u ? 1u : 0u;
         if (t->chunk_particles && t->chunk_particles != c.tune.chunk) {

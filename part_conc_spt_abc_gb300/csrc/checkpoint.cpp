@@ -13,11 +13,17 @@
  * std::mt19937 stream and in-flight queues make a resume inexact).
  *
  * Blob layout (little-endian, as the host stores it): a header
- * {magic, version, N, P, C, Z, V, R, B, model, seed, bytes}, the scalar
- * counters, then theta, theta_new [N*P], w, wcum, dist, dist_new [N] (f64),
- * factor [P*P] (f64), next_trial, pending, accepted [N] (u32).
+ * {magic, version, N, P, C, Z, V, R, B, model, fingerprint, seed, bytes},
+ * the scalar counters, then theta, theta_new [N*P], w, wcum, dist, dist_new
+ * [N] (f64), factor [P*P] (f64), next_trial, pending, accepted [N] (u32).
+ * The fingerprint is a 32-bit FNV-1a hash of every job parameter that
+ * shapes the job's future (all of pcs_params but max_generations, which a
+ * resumed job takes from its own parameters) and of the observed data
+ * (detection area, frame interval, frame counts, K and DE); a checkpoint
+ * whose fingerprint differs from the loading job's is refused.
  */
 #include <cstring>
+#include <vector>
 
 #include "engine.h"
 
@@ -26,14 +32,53 @@ namespace pcs {
 namespace {
 
 const uint64_t kMagic = 0x31544B4353435000ull; /* "\0PCSCKT1" */
-const uint32_t kVersion = 1;
+const uint32_t kVersion = 2;
 
 struct CkptHeader {
     uint64_t magic;
-    uint32_t version, N, P, C, Z, V, R, B, model, pad;
+    uint32_t version, N, P, C, Z, V, R, B, model, fingerprint;
     uint64_t seed;
     uint64_t bytes;
 };
+
+/* FNV-1a, 32 bits, over explicit fields (no struct padding bytes) */
+struct Fnv {
+    uint32_t h = 2166136261u;
+    void bytes(const void* p, size_t n)
+    {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < n; ++i) {
+            h ^= c[i];
+            h *= 16777619u;
+        }
+    }
+    template <class T> void add(const T& v) { bytes(&v, sizeof v); }
+};
+
+uint32_t job_fingerprint(const pcs_params& p, double ax, double ay, double deltat, const std::vector<uint32_t>& frames,
+                         const std::vector<uint32_t>& K, const std::vector<double>& DE)
+{
+    Fnv f;
+    f.add(p.model);
+    f.add(p.weighting_scheme);
+    f.add(p.component_count);
+    f.add(p.kmin);
+    f.add(p.de_bin_count);
+    f.add(p.abc_sample_count);
+    f.add(p.avg_trial_count);
+    f.add(p.gamma_adaptive);
+    const double d[] = {p.Lx, p.Ly, p.Lz, p.gamma_initial, p.delta_gamma, p.ub_de, p.lb_m, p.ub_m, p.lb_s, p.ub_s,
+                        p.lb_c, p.ub_c, p.lb_az, p.ub_az, p.temperature, p.viscosity, p.quantile, ax, ay, deltat};
+    f.bytes(d, sizeof d);
+    f.add(p.schedule);
+    f.add(p.perturbation);
+    f.add(p.reference_initial_gamma);
+    f.add(p.distance_double);
+    f.bytes(frames.data(), frames.size() * sizeof(uint32_t));
+    f.bytes(K.data(), K.size() * sizeof(uint32_t));
+    f.bytes(DE.data(), DE.size() * sizeof(double));
+    return f.h;
+}
 
 struct CkptScalars {
     double gamma;
@@ -86,6 +131,7 @@ void Job::save_state(void* buf) const
     h.R = R;
     h.B = B;
     h.model = (uint32_t)p.model;
+    h.fingerprint = job_fingerprint(p, ax, ay, deltat, frames, K, DE);
     h.seed = seed;
     h.bytes = checkpoint_bytes();
     std::memcpy(p8, &h, sizeof h);
@@ -129,6 +175,9 @@ void Job::load_state(const void* buf, size_t bytes)
         h.model != (uint32_t)p.model || h.seed != seed)
         throw Error(PCS_ERR_INVALID_ARGUMENT,
                     "checkpoint was taken from a job with other parameters, observed data shape or seed");
+    if (h.fingerprint != job_fingerprint(p, ax, ay, deltat, frames, K, DE))
+        throw Error(PCS_ERR_INVALID_ARGUMENT,
+                    "checkpoint was taken from a job with other parameters or observed data");
     if (h.bytes != checkpoint_bytes() || bytes < h.bytes) throw Error(PCS_ERR_INVALID_ARGUMENT, "checkpoint size mismatch");
     p8 += sizeof h;
     CkptScalars c;

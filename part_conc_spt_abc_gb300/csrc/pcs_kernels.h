@@ -48,6 +48,8 @@ struct SimLaunch {
 };
 
 cudaError_t launch_simulate(const SimArgs& a, const SimLaunch& l, cudaStream_t st);
+/* largest CTA the forward model's build for `ppt` walkers per thread launches */
+__host__ __device__ constexpr uint32_t sim_max_block(int ppt) { return ppt == 1 ? 1024u : (ppt == 2 ? 512u : 256u); }
 int simulate_occupancy(const SimLaunch& l, uint32_t tile_words);
 cudaError_t launch_debug_stream(uint64_t seed, uint32_t slot, uint32_t gen, uint32_t trial,
                                 uint32_t particle, uint32_t block, uint32_t* d_out,

@@ -29,3 +29,40 @@ def test_peaks_and_roofline_constants():
     # 0.75 Philox calls x 80 + 1.5 Box-Muller pairs x 14 + 32 walk operations
     assert b.OPS_PER_STEP == 0.75 * 80 + 1.5 * 14 + 32
     assert b.DIST_BYTES_PER_CELL == 12
+
+
+def test_job_sequence_steps_only_jobs_with_work():
+    """Each step of the bench's job sequence advances a job that has not
+    finished; a finished job hands over to the next seed, created on
+    demand once the prepared ones are used."""
+    from types import SimpleNamespace
+    b = load_bench()
+    made = []
+
+    class FakeSim:
+        def __init__(self, ctx, inp, seed):
+            self.seed, self.left, self.closed = seed, 3 + seed % 2, False
+            made.append(self)
+
+        def step(self):
+            assert self.left > 0, "stepped a finished job"
+            self.left -= 1
+            return self.left == 0
+
+        def info(self):
+            return SimpleNamespace(particle_steps=10 * (3 + self.seed % 2 - self.left), simulations=0, accepted=0)
+
+        def close(self):
+            self.closed = True
+
+    P = SimpleNamespace(make_simulation=FakeSim)
+    seq = b.JobSequence(P, None, None, seed0=1, prepare=2)
+    assert len(made) == 2
+    for _ in range(11):
+        seq.step()
+    assert seq.jobs_finished == 3 and len(made) == 3  # seeds 1 (4 steps), 2 (3), 3 (4): 11 steps
+    seq.step()  # the fourth job, made on demand
+    assert len(made) == 4 and seq.jobs_finished == 3
+    assert seq.totals()[0] == 120
+    seq.close()
+    assert all(s.closed for s in made)

@@ -85,3 +85,37 @@ def test_checkpoint_refusals(pcs, ctx):
     with pytest.raises(pcs.PcsError):
         wrong_shape.restore(ck[:100])
     wrong_shape.close()
+
+
+def test_checkpoint_refused_by_other_parameters_or_observed_data(pcs, ctx):
+    """Same shape and seed, but other prior bounds, frame interval,
+    weighting, schedule quantile or observed data: refused.  Another
+    generation cap is accepted (the resumed job obeys its own)."""
+    import copy
+    inp, _ = small_input(pcs, C=1, pop=32)
+    a = pcs.make_simulation(ctx, inp, 3)
+    a.step()
+    ck = a.checkpoint()
+    a.close()
+
+    def variant(edit):
+        v = copy.copy(inp)
+        v.params = copy.copy(inp.params)
+        edit(v)
+        return v
+
+    def set_param(name, value):
+        return lambda v: setattr(v.params, name, value)
+
+    refused = [set_param("ub_m", inp.params.ub_m * 1.01), set_param("lb_c", inp.params.lb_c * 2),
+               set_param("weighting_scheme", 1), set_param("quantile", 0.4),
+               lambda v: setattr(v, "deltat", inp.deltat * 1.001),
+               lambda v: setattr(v, "DE", np.asarray(inp.DE) * 1.0000001)]
+    for edit in refused:
+        b = pcs.make_simulation(ctx, variant(edit), 3)
+        with pytest.raises(pcs.PcsError, match="other parameters or observed data"):
+            b.restore(ck)
+        b.close()
+    c = pcs.make_simulation(ctx, variant(set_param("max_generations", 2)), 3)
+    c.restore(ck)
+    c.close()

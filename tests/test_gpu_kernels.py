@@ -236,6 +236,7 @@ def test_philox_determinism_and_independence(pcs, ctx, oracle, walk):
     # independent of the launch shape
     for kw in [dict(block_size=128, particles_per_thread=1), dict(block_size=512, particles_per_thread=2),
                dict(block_size=256, particles_per_thread=4, warp_aggregate=1),
+               dict(block_size=256, particles_per_thread=8),
                dict(block_size=256, particles_per_thread=1, hist_tile_rows=0xFFFFFFFF),  # warp slices
                dict(block_size=1024, particles_per_thread=1, hist_tile_rows=0xFFFFFFFF, warp_aggregate=1)]:
         ctx.set_tuning(**kw)
@@ -250,3 +251,10 @@ def test_bad_arguments_raise(pcs, ctx, oracle):
     setup.rows = 5  # rows must exceed the frame count
     with pytest.raises(pcs.PcsError):
         pcs.simulate_hist(ctx, setup, run)
+    # a launch shape the build for that walker count cannot run is refused
+    # up front, not at launch
+    with pytest.raises(pcs.PcsError, match="walkers per thread"):
+        ctx.set_tuning(block_size=1024, particles_per_thread=2)
+    with pytest.raises(pcs.PcsError, match="1, 2, 4 or 8"):
+        ctx.set_tuning(particles_per_thread=3)
+    ctx.set_tuning(block_size=256, particles_per_thread=1)

@@ -71,7 +71,8 @@ def test_results_do_not_depend_on_batching(pcs, ctx, walk):
     ref_out, ref_info = run_job(pcs, ctx, inp, 9, 3)
     settings = [dict(max_speculation=1), dict(max_speculation=3, block_size=128, particles_per_thread=2),
                 dict(round_capacity=200, max_speculation=64),
-                dict(max_speculation=4096, block_size=512, particles_per_thread=4, hist_tile_rows=8,
+                dict(block_size=128, particles_per_thread=8),
+                dict(max_speculation=4096, block_size=256, particles_per_thread=4, hist_tile_rows=8,
                      warp_aggregate=1),
                 dict(round_fill=0xFFFFFFFF), dict(round_fill=3000000), dict(job_order=2),
                 # no shared-memory tile: each warp takes its own slices of the work items

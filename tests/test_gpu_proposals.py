@@ -95,6 +95,7 @@ def check_rounds(pcs, ctx, oracle, inp, seed, rounds):
 def test_lognormal_proposals_match_oracle(pcs, ctx, oracle, perturbation):
     inp, _ = small_input(pcs, C=2, pop=64)
     inp.params.perturbation = perturbation
+    inp.params.lb_c = 1e6  # particles/ml: Poisson means from ~0.6 per video up
     n, lam = check_rounds(pcs, ctx, oracle, inp, 23, 4)
     assert n >= 64
     # both Poisson samplers ran: inversion below a mean of 12, PTRS above
