@@ -638,6 +638,8 @@ def main():
                     help="serve: capacity order among jobs (1 admission, 2 least remaining work; 0 library default)")
     ap.add_argument("--cmp-jobs", type=int, default=4, help="serve: jobs in the equal-work comparison")
     ap.add_argument("--cmp-generations", type=int, default=6, help="serve: generations per compared job")
+    ap.add_argument("--pmc-pop4096", action="store_true",
+                    help="only the PMC step's time per generation at population 4096, as its own line")
     ap.add_argument("--headline-only", action="store_true",
                     help="configuration 1 alone: no configuration 2 / 3 slices, PMC timing or serving stream")
     args = ap.parse_args()
@@ -649,6 +651,12 @@ def main():
         return
     if args.serve:
         run_serve(args, local, world)
+        return
+    if args.pmc_pop4096:
+        import part_conc_spt_abc_gb300 as P
+        if rank == 0:
+            print(json.dumps({"metric": "PMC step ms per generation at population 4096",
+                              **pmc_at_pop4096(P, local)}), flush=True)
         return
 
     import part_conc_spt_abc_gb300 as P

@@ -338,6 +338,8 @@ pcs_status pcs_job_destroy(pcs_job* job)
         Ctx& c = *j.ctx;
         PCS_CUDA(cudaSetDevice(c.device));
         if (j.slot >= 0) c.retire(&j);
+        /* a served job destroyed before it finished gives its arena back */
+        if (j.mem_counted) c.mem_used -= std::min<uint64_t>(c.mem_used, j.arena_bytes());
         c.queue.erase(std::remove(c.queue.begin(), c.queue.end(), &j), c.queue.end());
         delete job;
     });
@@ -496,6 +498,7 @@ pcs_status pcs_serve_step(pcs_ctx* ctx, uint32_t* active)
             c.queue.pop_front();
             c.admit(j);
             c.mem_used += j->arena_bytes();
+            j->mem_counted = true;
         }
         uint32_t running = 0;
         for (Job* t : c.table)
@@ -509,6 +512,7 @@ pcs_status pcs_serve_step(pcs_ctx* ctx, uint32_t* active)
                     t->finished = true;
                     t->t_done = std::chrono::steady_clock::now();
                     c.mem_used -= std::min<uint64_t>(c.mem_used, t->arena_bytes());
+                    t->mem_counted = false;
                     c.retire(t);
                 }
             }

@@ -134,6 +134,7 @@ struct Job {
     bool initialised = false;
     bool finished = false;
     bool in_serve = false;
+    bool mem_counted = false; /* its arena is counted in the context's serve memory use */
     double device_ms = 0.0;
     std::chrono::steady_clock::time_point t_submit, t_done;
 

@@ -538,19 +538,85 @@ __device__ __forceinline__ void kernel_sum_one_(const JobPmcDev& pm, uint32_t an
 }
 
 /* ----------------------------------------------------------------------- */
-/* rank of element i in (value, index) order */
-__device__ uint32_t select_rank_(const double* x, uint32_t N, uint32_t target, double* out_shared)
+/* Order-preserving map of a double to an unsigned key (negative values:
+ * all bits flipped; others: the sign bit set), and back. */
+__device__ __forceinline__ unsigned long long order_key_(double x)
 {
-    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
-        const double xi = x[i];
-        uint32_t rank = 0;
-        for (uint32_t t = 0; t < N; ++t) {
-            const double xt = x[t];
-            rank += (xt < xi || (xt == xi && t < i)) ? 1u : 0u;
-        }
-        if (rank == target) *out_shared = xi;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ double from_order_key_(unsigned long long k)
+{
+    const unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+struct SelectShared {
+    uint32_t hist[256];
+    unsigned long long prefix, mask;
+    uint32_t target;
+};
+
+/* The value at position `target` (0-based) of x[0..N) in ascending order
+ * (nth_element's result, simulation_impl.inl:819-829), by one block: a
+ * radix select over the order-preserving keys, eight passes of 8-bit
+ * digits from the top; each pass counts the candidates' digits in shared
+ * memory (warp-aggregated atomics) and keeps the digit whose bucket holds
+ * the target rank.  O(8 N) work instead of comparing all pairs. */
+__device__ double select_rank_(const double* x, uint32_t N, uint32_t target, SelectShared& sh)
+{
+    const uint32_t tid = threadIdx.x, bd = blockDim.x, lane = tid & 31u;
+    if (tid == 0) {
+        sh.prefix = 0ull;
+        sh.mask = 0ull;
+        sh.target = target;
     }
-    return 0;
+    for (int shift = 56; shift >= 0; shift -= 8) {
+        for (uint32_t b = tid; b < 256u; b += bd) sh.hist[b] = 0u;
+        __syncthreads();
+        const unsigned long long prefix = sh.prefix, mask = sh.mask;
+        for (uint32_t base = 0; base < N; base += bd) { /* the same trip count for every thread */
+            const uint32_t i = base + tid;
+            uint32_t digit = 256u; /* no candidate */
+            if (i < N) {
+                const unsigned long long k = order_key_(x[i]);
+                if ((k & mask) == prefix) digit = (uint32_t)(k >> shift) & 255u;
+            }
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, digit);
+            if (digit < 256u && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&sh.hist[digit], (uint32_t)__popc(peers));
+        }
+        __syncthreads();
+        if (tid < 32u) {
+            /* warp 0: lane l owns digits 8l .. 8l+7; find the digit holding the target */
+            uint32_t c[8], own = 0u;
+            for (int t = 0; t < 8; ++t) {
+                c[t] = sh.hist[8u * lane + t];
+                own += c[t];
+            }
+            uint32_t incl = own;
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+                if ((int)lane >= d) incl += v;
+            }
+            const uint32_t tgt = sh.target, excl = incl - own;
+            if (tgt >= excl && tgt < incl) { /* exactly one lane */
+                uint32_t run = excl, dsel = 8u * lane;
+                for (int t = 0; t < 8; ++t) {
+                    if (tgt < run + c[t]) {
+                        dsel = 8u * lane + (uint32_t)t;
+                        break;
+                    }
+                    run += c[t];
+                }
+                sh.target = tgt - run;
+                sh.prefix |= (unsigned long long)dsel << shift;
+                sh.mask |= 255ull << shift;
+            }
+        }
+        __syncthreads();
+    }
+    return from_order_key_(sh.prefix);
 }
 
 __device__ double block_sum_(double v, double* s_red)
@@ -620,6 +686,7 @@ __global__ void __launch_bounds__(1024) k_finalize(PmcArgs a)
     __shared__ double s_sel;
     __shared__ double s_mean[PCS_MAX_P];
     __shared__ double s_cov[PCS_MAX_P * PCS_MAX_P];
+    __shared__ SelectShared s_select;
     const uint32_t j = blockIdx.x;
     RoundDev* rd = a.round;
     if (j >= rd->n_jobs) return;
@@ -631,12 +698,9 @@ __global__ void __launch_bounds__(1024) k_finalize(PmcArgs a)
     bool commit = true;
     if (pm.generation == 0u) {
         /* prior pass: gamma_0 from the median distance (compute_initial_gamma_ :819-829) */
-        if (tid == 0) s_sel = 0.0;
-        __syncthreads();
         const uint32_t target = (pm.schedule == 1u) ? min(N - 1u, (uint32_t)floor(pm.quantile * N)) : N / 2u;
-        select_rank_(pm.dist_new, N, target, &s_sel);
-        __syncthreads();
-        if (tid == 0) pm.gamma = s_sel;
+        const double g0 = select_rank_(pm.dist_new, N, target, s_select);
+        if (tid == 0) pm.gamma = g0;
         /* the reference keeps the prior population as drawn; the quantile
          * schedule keeps its distances as the generation-0 distances */
         for (uint32_t i = tid; i < N; i += bd) pm.dist[i] = (pm.schedule == 1u) ? pm.dist_new[i] : 0.0;
@@ -764,10 +828,9 @@ __global__ void __launch_bounds__(1024) k_finalize(PmcArgs a)
 
     /* epsilon for the next generation */
     if (pm.schedule == 1u && pm.generation > 0u) {
-        if (tid == 0) s_sel = 0.0;
-        __syncthreads();
         const uint32_t target = min(N - 1u, (uint32_t)floor(pm.quantile * N));
-        select_rank_(pm.dist, N, target, &s_sel);
+        const double eps = select_rank_(pm.dist, N, target, s_select);
+        if (tid == 0) s_sel = eps;
         __syncthreads();
     }
     if (tid == 0) {

@@ -169,6 +169,31 @@ def test_serve_mixed_shapes_alone_equals_mix(pcs, ctx):
         s.close()
 
 
+def test_destroyed_served_job_gives_its_memory_back(pcs):
+    """A served job destroyed before it finishes no longer counts against
+    the memory cap: under a cap that holds one job, a second job is
+    admitted after the first is destroyed mid-run."""
+    c2 = pcs.Context(0)
+    try:
+        jobs = [small_input(pcs, seed=s, C=1, pop=48)[0] for s in range(2)]
+        hist_b = c2.tuning.round_capacity * (61 * 48) * 4
+        srv = pcs.Server(c2, memory_cap=hist_b + 48000)
+        a = pcs.make_simulation(c2, jobs[0], 1)
+        srv.submit(a)
+        srv.step()
+        assert not srv.finished(a)
+        a.close()
+        b = pcs.make_simulation(c2, jobs[1], 2)
+        srv.submit(b)
+        for _ in range(100000):
+            if srv.step() == 0:
+                break
+        assert srv.finished(b)
+        b.close()
+    finally:
+        c2.close()
+
+
 def test_serve_memory_cap(pcs, ctx):
     """With a cap that holds one job's arena and the round histograms but not
     two, jobs are admitted one after another and give the same results as

@@ -109,7 +109,7 @@ def test_discrete_proposals_match_oracle(pcs, ctx, oracle, model):
     assert n >= 64 and (lam >= 12).any()
 
 
-@pytest.mark.parametrize("N", [64, 63])
+@pytest.mark.parametrize("N", [64, 63, 4097])
 def test_initial_gamma_is_the_upper_median_of_prior_distances(pcs, ctx, N):
     """Delta schedule (the reference's): after the prior pass gamma_0 is the
     element of rank N/2 of the prior population's distances
@@ -131,16 +131,20 @@ def test_initial_gamma_is_the_upper_median_of_prior_distances(pcs, ctx, N):
         sim.close()
 
 
-def test_quantile_threshold_after_prior_pass(pcs, ctx):
+@pytest.mark.parametrize("N,q", [(50, 0.5), (3001, 0.3)])
+def test_quantile_threshold_after_prior_pass(pcs, ctx, N, q):
     """Quantile schedule: epsilon for generation 1 is the element of rank
-    floor(q N) of the prior distances, with no delta step."""
-    inp, _ = small_input(pcs, C=1, pop=50)
-    q = inp.params.quantile
+    floor(q N) of the prior distances, with no delta step; so is the next
+    generation's, from the committed distances."""
+    inp, _ = small_input(pcs, C=1, pop=N)
+    inp.params.quantile = q
     sim = pcs.make_simulation(ctx, inp, 43)
     try:
         sim.step()
-        st = parse(sim.checkpoint(), 50, sim.info().param_count)
-        d = st["dist_new"]
-        assert sim.info().gamma == np.sort(d)[min(49, int(np.floor(q * 50)))]
+        st = parse(sim.checkpoint(), N, sim.info().param_count)
+        assert sim.info().gamma == np.sort(st["dist_new"])[min(N - 1, int(np.floor(q * N)))]
+        if not sim.step():
+            st = parse(sim.checkpoint(), N, sim.info().param_count)
+            assert sim.info().gamma == np.sort(st["dist"])[min(N - 1, int(np.floor(q * N)))]
     finally:
         sim.close()
