@@ -654,7 +654,7 @@ void Ctx::run_round(double* ms_out)
         *h_err = 0;
         PCS_CUDA(cudaMemset(err.p, 0, 16));
         char buf[160];
-        std::snprintf(buf, sizeof buf, "device error word 0x%x (1 hist bounds, 2 component, 4 items, 8 counts, 16 hist cap, 32 rows, 64 param)", bits);
+        std::snprintf(buf, sizeof buf, "device error word 0x%x (1 hist bounds, 2 component, 4 items, 8 counts, 16 hist cap, 32 rows, 64 param, 128 copy wait)", bits);
         throw Error(PCS_ERR_DEVICE, buf);
     }
     for (size_t i = 0; i < table.size(); ++i)

@@ -202,33 +202,97 @@ __global__ void __launch_bounds__(1024, 1) k_distance(DistArgs a)
     }
 }
 
+__device__ __forceinline__ uint32_t pick4_(const uint4& v, uint32_t i)
+{
+    return i == 0u ? v.x : (i == 1u ? v.y : (i == 2u ? v.z : v.w));
+}
+
 /* Strip kernel: 16 warps, full-height strips of 32 DE columns, a persistent
  * CTA walking the (proposal, strip) sequence blockIdx.x, blockIdx.x + grid,
  * ... strip by strip.
  *
- * Copy: warp w owns a contiguous segment of ceil(R/16) rows; lane l copies
- * column c0+l of those rows into the tile with 4-byte cp.async (any B, any
- * offset; columns past B are zero-filled).  With two tiles (db) the copies of
- * the next strip -- or of the next proposal's first strip -- are in flight
- * while the current strip is computed, so the histogram streams from HBM
- * without a round trip per strip; with one tile (tall histograms) the copies
- * of a strip are issued together, one round trip per strip.
- * Phase A1: each lane sums its own copied cells (column totals of the
- * segment) and writes zeros back to the histogram, as K_distance does.
+ * Copy: warp w owns a contiguous segment of ceil(R/16) rows, lane i the
+ * rows rb+i, rb+i+32, ... of it.  A row's 32 cells (128 bytes) move with
+ * one bulk copy (cp.async.bulk, the TMA unit) completing on the tile's
+ * mbarrier, when source, destination and size are 16-byte aligned (B a
+ * multiple of 4 and an aligned histogram; every copy is checked before it
+ * is issued); cells past B are zero-filled with plain stores.  Other rows
+ * take 4-byte cp.async per cell (any B, any offset).  Every thread arrives
+ * on the tile's mbarrier once per fill with the bytes of its bulk copies,
+ * so a waiter passes only when all copies of the strip have landed; the
+ * wait is bounded (error bit 0x80 and a clean exit when it runs out).  With
+ * two tiles (db) the copies of the next strip -- or of the next proposal's
+ * first strip -- are in flight while the current strip is computed; with
+ * one tile (tall histograms) the copies of a strip are issued together.
+ * Phase A1: each lane sums column c0+l of its warp's segment (column totals
+ * of the segment) and writes zeros back to the histogram, as K_distance
+ * does.
  * Phase A2: lane l runs down column c0+l of the segment from the totals of
  * the segments above (column prefix), then lane j runs across row rb+j from
- * the row's carry of the strips to its left (row prefix): the tile holds the
- * 2-D prefix sums after per-lane chains through shared memory, no shuffles
- * (the 33-word pitch keeps both passes free of bank conflicts).
+ * the row's carry of the strips to its left (row prefix, 128-bit shared
+ * loads and stores): the tile holds the 2-D prefix sums after per-lane
+ * chains through shared memory, no shuffles.
  * Phase B: warp w reads two columns of the strip, c0+w for logical warp w
  * and c0+w+16 for logical warp w+16 of the reference's 32x32 launch, so
  * every lane keeps the reference's per-lane sums in two accumulators; the
  * observed cumulative histogram of four 32-row groups is requested at once.
  * SSD: also accumulate the exact integer sum of squares (128-bit per lane);
  * the PMC rounds do not ask for it, the parity entry point does.
- * R x 33 words per tile: two tiles and two CTAs per SM up to ~420 rows. */
+ * Tile rows are 36 words (144 bytes): 16-byte aligned for the bulk copies,
+ * and with 128-bit shared accesses (row pass, and the 16-byte chunk holding
+ * a column in phase B) eight consecutive rows fall in eight different
+ * bank groups, so both passes are free of bank conflicts.  R x 36 words per
+ * tile: two tiles and two CTAs per SM up to ~385 rows. */
 const uint32_t kStripThreads = 512;
 const int kStripRefGroups = 4;
+const uint32_t kSPitch = 36;                 /* strip tile row pitch (words) */
+const uint32_t kMbarWaitLimit = 1u << 22;    /* try_wait rounds before a wait is given up */
+
+__device__ __forceinline__ uint32_t smem_u32_(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init_(uint64_t* m, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared.b64 [%0], %1;\n" ::"r"(smem_u32_(m)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init_fence_() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_arrive_expect_tx_(uint64_t* m, uint32_t bytes)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}\n" ::"r"(smem_u32_(m)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait_(uint64_t* m, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+                 : "=r"(done)
+                 : "r"(smem_u32_(m)), "r"(parity)
+                 : "memory");
+    return done != 0u;
+}
+
+/* bounded wait for a phase of the mbarrier */
+__device__ __forceinline__ bool mbar_wait_(uint64_t* m, uint32_t parity)
+{
+    for (uint32_t it = 0; it < kMbarWaitLimit; ++it)
+        if (mbar_try_wait_(m, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void bulk_copy_(void* dst, const void* src, uint32_t bytes, uint64_t* m)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32_(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32_(m))
+                 : "memory");
+}
+
+/* orders this thread's earlier generic shared-memory accesses before later
+ * async-proxy (bulk copy) writes to the same memory */
+__device__ __forceinline__ void fence_proxy_async_() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
 __device__ __forceinline__ void cp_async4_(uint32_t* dst, const uint32_t* src, bool valid)
 {
@@ -242,41 +306,69 @@ __device__ __forceinline__ void cp_async_commit_() { asm volatile("cp.async.comm
 template <int N>
 __device__ __forceinline__ void cp_async_wait_() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-/* Issue this lane's copies of strip c0 of proposal p into tile T. */
+__device__ __forceinline__ bool aligned16_(const void* p) { return ((uintptr_t)p & 15u) == 0u; }
+
+/* This thread's copies of strip c0 of proposal p into tile T, and its one
+ * arrival on the tile's mbarrier (with the bytes of its bulk copies). */
 __device__ __forceinline__ void strip_copy_(const DistArgs& a, uint32_t p, uint32_t c0, uint32_t* T, uint32_t w,
-                                            uint32_t l)
+                                            uint32_t l, uint64_t* mbar)
 {
     const uint32_t job = a.props[p].job;
     const uint32_t R = a.jobs[job].R, B = a.jobs[job].B;
-    if (R > a.max_rows) return;
+    const bool ok = R <= a.max_rows;
     const uint32_t* hist = a.hist + a.props[p].hist_off;
     const uint32_t seg = (R + 15u) / 16u;
-    const uint32_t rb = min(R, w * seg), re = min(R, rb + seg);
-    const uint32_t c = c0 + l;
-    const bool cin = c < B;
-    for (uint32_t r = rb; r < re; ++r) cp_async4_(T + r * kPad + l, cin ? hist + (uint64_t)r * B + c : hist, cin);
+    const uint32_t rb = ok ? min(R, w * seg) : 0u, re = ok ? min(R, rb + seg) : 0u;
+    const uint32_t n = B > c0 ? min(32u, B - c0) : 0u; /* cells of this strip in a row */
+    const bool bulk_shape = n > 0u && (n & 3u) == 0u;
+    uint32_t bytes = 0u;
+    if (bulk_shape)
+        for (uint32_t r = rb + l; r < re; r += 32u)
+            if (aligned16_(hist + (uint64_t)r * B + c0) && aligned16_(T + r * kSPitch)) bytes += 4u * n;
+    mbar_arrive_expect_tx_(mbar, bytes);
+    for (uint32_t r = rb + l; r < re; r += 32u) {
+        const uint32_t* src = hist + (uint64_t)r * B + c0;
+        uint32_t* dst = T + r * kSPitch;
+        if (bulk_shape && aligned16_(src) && aligned16_(dst)) {
+            bulk_copy_(dst, src, 4u * n, mbar);
+            for (uint32_t c = n; c < 32u; ++c) dst[c] = 0u;
+        } else {
+            for (uint32_t c = 0; c < 32u; ++c) cp_async4_(dst + c, c < n ? src + c : hist, c < n);
+        }
+    }
 }
 
 template <bool F64, bool SSD>
 __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t db)
 {
-    extern __shared__ uint32_t s_mem[];
-    uint32_t* carry = s_mem;                              /* [max_rows] */
-    uint32_t* tiles = s_mem + a.max_rows;                 /* [1 + db][max_rows][kPad] */
-    const uint32_t tile_words = a.max_rows * kPad;
+    extern __shared__ __align__(16) uint32_t s_mem[];
+    const uint32_t tile_words = a.max_rows * kSPitch;
+    /* 16-byte aligned tiles (the launch reserves 16 bytes for this) */
+    uint32_t* tiles = s_mem + ((16u - (smem_u32_(s_mem) & 15u)) & 15u) / 4u; /* [1 + db][max_rows][kSPitch] */
+    uint32_t* carry = s_mem + (1u + db) * tile_words;     /* [max_rows] */
     __shared__ float s_tot[32];
     __shared__ double s_tot64[32];
     __shared__ uint64_t s_hi[32], s_lo[32];
     __shared__ uint32_t s_col[16][32]; /* column totals of each warp's row segment */
+    __shared__ __align__(8) uint64_t s_mbar[2];
+    __shared__ uint32_t s_abort;
 
     const uint32_t tid = threadIdx.x;
     const uint32_t w = tid >> 5, l = tid & 31u;
     const uint32_t M = *a.n_props;
     uint32_t p = blockIdx.x;
     if (p >= M) return;
+    if (tid == 0) {
+        mbar_init_(&s_mbar[0], kStripThreads);
+        mbar_init_(&s_mbar[1], kStripThreads);
+        mbar_init_fence_();
+        s_abort = 0u;
+    }
+    __syncthreads();
 
-    uint32_t c0 = 0, cur = 0;
-    strip_copy_(a, p, 0u, tiles, w, l);
+    uint32_t c0 = 0, cur = 0, parity = 0u; /* parity bit b: the phase of tile b's next fill */
+    uint32_t pending = 1u;                  /* bit b: tile b has a fill in flight */
+    strip_copy_(a, p, 0u, tiles, w, l, &s_mbar[0]);
     cp_async_commit_();
 
     float acc0 = 0.0f, acc1 = 0.0f;
@@ -295,14 +387,24 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
         }
         const bool has_next = pn < M;
         if (db) {
-            if (has_next) strip_copy_(a, pn, cn, tiles + (cur ^ 1u) * tile_words, w, l);
+            if (has_next) {
+                strip_copy_(a, pn, cn, tiles + (cur ^ 1u) * tile_words, w, l, &s_mbar[cur ^ 1u]);
+                pending |= 1u << (cur ^ 1u);
+            }
             cp_async_commit_();
-            cp_async_wait_<1>(); /* this lane's copies of the current strip have landed */
+            cp_async_wait_<1>(); /* this thread's 4-byte copies of the current strip have landed */
         } else {
             cp_async_wait_<0>();
         }
+        /* the current strip's bulk copies (all threads' arrivals and bytes) */
+        if (!mbar_wait_(&s_mbar[cur], (parity >> cur) & 1u)) {
+            atomicOr(a.err, PCS_ERRBIT_TIMEOUT);
+            s_abort = 1u;
+        }
+        parity ^= 1u << cur;
+        pending &= ~(1u << cur);
+        __syncwarp(); /* rows copied by other lanes of this warp (4-byte copies, zero fills) */
         uint32_t* T = tiles + cur * tile_words;
-
         if (!ok) {
             if (tid == 0) {
                 atomicOr(a.err, PCS_ERRBIT_ROWS);
@@ -320,31 +422,34 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
             uint32_t coltot = 0u;
 #pragma unroll 4
             for (uint32_t r = rb; r < re; ++r) {
-                coltot += T[r * kPad + l];
+                coltot += T[r * kSPitch + l];
                 if (cin) __stcs(hist + (uint64_t)r * B + c, 0u);
             }
             s_col[w][l] = coltot;
             __syncthreads();
+            if (s_abort) break; /* a copy wait ran out (error word set) */
             /* phase A2: column prefix down the segment, then row prefix across
              * the strip: the tile holds the 2-D prefix sums */
             uint32_t run = 0u;
             for (uint32_t q = 0; q < w; ++q) run += s_col[q][l];
 #pragma unroll 4
             for (uint32_t r = rb; r < re; ++r) {
-                run += T[r * kPad + l];
-                T[r * kPad + l] = run;
+                run += T[r * kSPitch + l];
+                T[r * kSPitch + l] = run;
             }
             __syncwarp();
             for (uint32_t r = rb + l; r < re; r += 32u) {
-                uint32_t* row = T + r * kPad;
-                uint32_t v[32];
-#pragma unroll
-                for (int j = 0; j < 32; ++j) v[j] = row[j];
+                uint4* row4 = reinterpret_cast<uint4*>(T + r * kSPitch);
                 uint32_t acc = c0 ? carry[r] : 0u;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    acc += v[j];
-                    row[j] = acc;
+                for (int j = 0; j < 8; ++j) {
+                    uint4 v = row4[j];
+                    v.x += acc;
+                    v.y += v.x;
+                    v.z += v.y;
+                    v.w += v.z;
+                    acc = v.w;
+                    row4[j] = v;
                 }
                 carry[r] = acc;
             }
@@ -367,7 +472,8 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
                     for (int g = 0; g < kStripRefGroups; ++g) {
                         const uint32_t r = rg + 32u * (uint32_t)g + l;
                         if (r < R) {
-                            const uint32_t sA = T[r * kPad + w];
+                            const uint4 chA = reinterpret_cast<const uint4*>(T + r * kSPitch)[w >> 2];
+                            const uint32_t sA = pick4_(chA, w & 3u);
                             const uint32_t refA = refAv[g];
                             const float ddA = __fsub_rn(__uint2float_rn(sA), __uint2float_rn(refA));
                             a2A = __fadd_rn(a2A, __fmul_rn(ddA, ddA));
@@ -381,7 +487,8 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
                             }
                             if (cum) cum[(uint64_t)r * B + colA] = sA;
                             if (inB) {
-                                const uint32_t sB = T[r * kPad + w + 16u];
+                                const uint4 chB = reinterpret_cast<const uint4*>(T + r * kSPitch)[(w >> 2) + 4u];
+                                const uint32_t sB = pick4_(chB, w & 3u);
                                 const uint32_t refB = refBv[g];
                                 const float ddB = __fsub_rn(__uint2float_rn(sB), __uint2float_rn(refB));
                                 a2B = __fadd_rn(a2B, __fmul_rn(ddB, ddB));
@@ -406,7 +513,8 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
                 }
             }
         }
-        __syncthreads(); /* the tile is free for the copies issued next */
+        fence_proxy_async_(); /* this tile's generic accesses before its next bulk fill */
+        __syncthreads();      /* the tile is free for the copies issued next */
 
         if (ok && c0 + 32u >= B) {
             /* last strip: reduce0 per logical warp (w and w + 16), then over
@@ -463,7 +571,8 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
         }
         if (!has_next) break;
         if (!db) {
-            strip_copy_(a, pn, cn, tiles, w, l);
+            strip_copy_(a, pn, cn, tiles, w, l, &s_mbar[0]);
+            pending |= 1u;
             cp_async_commit_();
         } else {
             cur ^= 1u;
@@ -472,14 +581,17 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
         c0 = cn;
     }
     cp_async_wait_<0>();
+    /* after a given-up wait: let the fills still in flight land (bounded) */
+    for (uint32_t b = 0; b < 2u; ++b)
+        if ((pending >> b) & 1u) mbar_wait_(&s_mbar[b], (parity >> b) & 1u);
 }
 
 static const size_t kStripSmemMax = 220u * 1024u;
 
-/* carry + one or two tiles */
+/* one or two tiles + carry + 16 bytes to align the tiles */
 static size_t strip_smem_bytes(uint32_t max_rows, bool db)
 {
-    return ((size_t)max_rows * (1u + (db ? 2u : 1u) * kPad)) * sizeof(uint32_t);
+    return ((size_t)max_rows * (1u + (db ? 2u : 1u) * kSPitch)) * sizeof(uint32_t) + 16u;
 }
 
 static bool use_strip(uint32_t max_rows) { return strip_smem_bytes(max_rows, false) <= kStripSmemMax; }

@@ -179,7 +179,7 @@ extern "C" pcs_status pcs_scan_distance_noalloc(uint32_t* d_hist, const uint32_t
     if (e != cudaSuccess) return fail_(PCS_ERR_CUDA, std::string("distance kernel: ") + cudaGetErrorString(e));
     if (word) {
         char buf[96];
-        snprintf(buf, sizeof buf, "distance kernel raised device error word 0x%x (32: histogram rows)", word);
+        snprintf(buf, sizeof buf, "distance kernel raised device error word 0x%x (32: histogram rows, 128: copy wait)", word);
         return fail_(PCS_ERR_DEVICE, buf);
     }
     return fail_(PCS_OK, "");

@@ -17,6 +17,7 @@
 #define PCS_ERRBIT_HISTCAP 0x10u      /* histogram capacity exceeded */
 #define PCS_ERRBIT_ROWS 0x20u         /* distance kernel: rows exceed shared memory */
 #define PCS_ERRBIT_PARAM 0x40u        /* non-finite parameter or weight */
+#define PCS_ERRBIT_TIMEOUT 0x80u      /* distance kernel: a copy wait ran out */
 
 namespace pcs {
 
