@@ -380,7 +380,7 @@ pcs_status pcs_scan_distance(pcs_ctx* ctx, const uint32_t* hist, const uint32_t*
  * allocator owns all device memory, services under a fixed device-memory
  * budget, and real-time loops where an allocation could stall on device
  * synchronisation cannot let a library call cudaMalloc; this variant takes device pointers
- * and keeps its working buffers (the transposed observed histogram and one
+ * and keeps its working buffers (a column-major copy of the observed histogram and one
  * descriptor per histogram) in a fixed __device__ array instead, calling no
  * allocator.  d_hist holds count x rows x bins counts and is reset to zero,
  * as K_distance resets its input; d_ref_sat is rows x bins; d_dist_f32 gets

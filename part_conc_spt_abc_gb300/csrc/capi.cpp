@@ -702,7 +702,8 @@ pcs_status pcs_scan_distance(pcs_ctx* ctx, const uint32_t* hist, const uint32_t*
         DevTmp t;
         std::vector<uint32_t> refT(RB);
         for (uint32_t r = 0; r < rows; ++r)
-            for (uint32_t b = 0; b < bins; ++b) refT[(uint64_t)b * rows + r] = ref_sat[(uint64_t)r * bins + b];
+            for (uint32_t b = 0; b < bins; ++b)
+                refT[pcs_sat_t_index(r, b, rows, bins)] = ref_sat[(uint64_t)r * bins + b];
         uint32_t* d_hist = t.get<uint32_t>(count * RB);
         uint32_t* d_ref = t.get<uint32_t>(RB);
         uint32_t* d_refT = t.get<uint32_t>(RB);
@@ -715,10 +716,14 @@ pcs_status pcs_scan_distance(pcs_ctx* ctx, const uint32_t* hist, const uint32_t*
         jd.B = bins;
         jd.ref_sat = d_ref;
         jd.ref_sat_t = d_refT;
+        TmapDev map;
+        jd.tmap_depth = encode_hist_tmap(&map, d_hist, rows, bins, count) ? count : 0u;
+        TmapDev* d_map = t.get<TmapDev>(1);
         std::vector<PropDev> props(count);
         for (uint32_t q = 0; q < count; ++q) {
             std::memset(&props[q], 0, sizeof(PropDev));
             props[q].hist_off = (uint64_t)q * RB;
+            props[q].hist_z = q;
         }
         JobDev* d_jobs = t.get<JobDev>(1);
         PropDev* d_props = t.get<PropDev>(count);
@@ -727,6 +732,7 @@ pcs_status pcs_scan_distance(pcs_ctx* ctx, const uint32_t* hist, const uint32_t*
         PCS_CUDA(cudaMemcpyAsync(d_ref, ref_sat, RB * 4, cudaMemcpyHostToDevice, st));
         PCS_CUDA(cudaMemcpyAsync(d_refT, refT.data(), RB * 4, cudaMemcpyHostToDevice, st));
         PCS_CUDA(cudaMemcpyAsync(d_jobs, &jd, sizeof jd, cudaMemcpyHostToDevice, st));
+        PCS_CUDA(cudaMemcpyAsync(d_map, &map, sizeof map, cudaMemcpyHostToDevice, st));
         PCS_CUDA(cudaMemcpyAsync(d_props, props.data(), sizeof(PropDev) * count, cudaMemcpyHostToDevice, st));
         PCS_CUDA(cudaMemcpyAsync(d_n, &count, 4, cudaMemcpyHostToDevice, st));
         DistArgs d{};
@@ -740,6 +746,7 @@ pcs_status pcs_scan_distance(pcs_ctx* ctx, const uint32_t* hist, const uint32_t*
         d.ssd = d_ssd;
         d.err = c.err.as<uint32_t>();
         d.max_rows = rows;
+        d.tmaps = d_map;
         PCS_CUDA(launch_distance(d, std::min<uint32_t>(count, (uint32_t)(distance_ctas_per_sm(rows) * c.sm_count)), st));
         if (cum_out) PCS_CUDA(cudaMemcpyAsync(cum_out, d_cum, count * RB * 4, cudaMemcpyDeviceToHost, st));
         PCS_CUDA(cudaMemcpyAsync(dist_f32, d_d32, count * 4, cudaMemcpyDeviceToHost, st));

@@ -475,7 +475,9 @@ void Ctx::ensure_round_buffers(uint32_t v_max, uint32_t max_rows, uint32_t max_n
         }
     items_need = std::max<uint64_t>(items_need, 2) * cap;
     if (items_need > (1ull << 31)) items_need = 1ull << 31;
-    const uint64_t hist_need = (uint64_t)cap * rb_max;
+    /* each job's histograms start at a multiple of its R x B words: up to one
+     * histogram of padding per job */
+    const uint64_t hist_need = ((uint64_t)cap + kMaxRoundJobs) * rb_max;
     if (rb.capacity == cap && rb.v_max >= v_max && rb.max_rows >= max_rows && rb.max_n >= max_n &&
         rb.items_cap >= items_need && rb.hist_cap >= hist_need)
         return;
@@ -497,6 +499,8 @@ void Ctx::ensure_round_buffers(uint32_t v_max, uint32_t max_rows, uint32_t max_n
     rb.dist32.alloc(sizeof(float) * (size_t)cap);
     rb.dist64.alloc(sizeof(double) * (size_t)cap);
     if (!rb.jobs.p) {
+        rb.tmaps.alloc(sizeof(TmapDev) * kMaxRoundJobs);
+        PCS_CUDA(cudaMemsetAsync(rb.tmaps.p, 0, sizeof(TmapDev) * kMaxRoundJobs, stream));
         rb.jobs.alloc(sizeof(JobDev) * kMaxRoundJobs);
         rb.pmc.alloc(sizeof(JobPmcDev) * kMaxRoundJobs);
         PCS_CUDA(cudaMemsetAsync(rb.jobs.p, 0, sizeof(JobDev) * kMaxRoundJobs, stream));
@@ -588,6 +592,7 @@ void Ctx::enqueue_round()
     d.ssd = nullptr;
     d.err = a.err;
     d.max_rows = rb.max_rows;
+    d.tmaps = rb.tmaps.as<TmapDev>();
     PCS_CUDA(cudaEventRecordWithFlags(ev_dist0, stream, cudaEventRecordExternal));
     PCS_CUDA(launch_distance(d, std::min<uint32_t>(rb.capacity, (uint32_t)(distance_ctas_per_sm(rb.max_rows) * sm_count)), stream));
     PCS_CUDA(cudaEventRecordWithFlags(ev_dist1, stream, cudaEventRecordExternal));
@@ -706,7 +711,18 @@ void Ctx::admit(Job* j)
         graph_dirty = true;
     }
     ensure_round_buffers(v_max, max_rows, max_n, rb_max);
-    PCS_CUDA(cudaMemcpyAsync(rb.jobs.as<JobDev>() + slot, &j->jd, sizeof(JobDev), cudaMemcpyHostToDevice, stream));
+    /* every job's tensor map: the histogram area may have moved */
+    std::vector<TmapDev> maps(table.size());
+    for (size_t i = 0; i < table.size(); ++i) {
+        Job* t = table[i];
+        if (!t) continue;
+        const uint64_t cells = (uint64_t)t->R * t->B;
+        const uint64_t depth = cells ? rb.hist_cap / cells : 0u;
+        t->jd.tmap_depth =
+            encode_hist_tmap(&maps[i], rb.hist.as<uint32_t>(), t->R, t->B, depth) ? (uint32_t)depth : 0u;
+        PCS_CUDA(cudaMemcpyAsync(rb.jobs.as<JobDev>() + i, &t->jd, sizeof(JobDev), cudaMemcpyHostToDevice, stream));
+    }
+    PCS_CUDA(cudaMemcpyAsync(rb.tmaps.p, maps.data(), sizeof(TmapDev) * maps.size(), cudaMemcpyHostToDevice, stream));
     PCS_CUDA(cudaMemcpyAsync(rb.pmc.as<JobPmcDev>() + slot, &j->status, sizeof(JobPmcDev), cudaMemcpyHostToDevice, stream));
     upload_table();
     PCS_CUDA(cudaStreamSynchronize(stream));

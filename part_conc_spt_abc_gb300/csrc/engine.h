@@ -71,6 +71,7 @@ struct RoundBufs {
     uint32_t capacity = 0, items_cap = 0, v_max = 0, max_rows = 0, max_n = 0;
     uint64_t counts_cap = 0, hist_cap = 0, ystride = 0;
     DevBuf round, props, theta_prop, counts, item_prop, hist, dist32, dist64, jobs, pmc;
+    DevBuf tmaps; /* [kMaxRoundJobs] TmapDev: each job's histogram tensor map over hist */
 };
 
 struct Ctx {

@@ -5,18 +5,18 @@
  * runs one 32x32 block per proposal over the whole R x B histogram twice
  * (row scans, then column scans accumulating (cum - ref)^2) and zeroes the
  * histogram for reuse.  Here one CTA per proposal streams the histogram in
- * strips of 32 DE columns through a shared-memory tile (row pitch 33 words,
- * so row-wise and column-wise accesses are both conflict-free):
- *   k_distance_strip (up to ~1650 rows, 512 threads): the whole strip
- *            height sits in the tile; phase A builds its 2-D prefix sums
- *            (coalesced 128-byte loads, zeros written back, per-lane column
- *            and row passes, per-row carry across strips in shared memory),
- *            phase B
- *            reads column c0+w for logical warp w while lane l accumulates
+ * strips of 32 DE columns through a shared-memory tile:
+ *   k_distance_strip (up to 1664 rows, 512 threads): the whole strip height
+ *            sits in a swizzled tile filled by TMA box copies; phase A
+ *            builds its 2-D prefix sums (zeros written back by box stores,
+ *            per-lane column and row passes, per-row carry across strips
+ *            in shared memory), phase B reads columns c0+2w, c0+2w+1 for
+ *            logical warps 2w, 2w+1 while lane l accumulates
  *            (float(cum) - float(ref))^2 for rows l, l+32, ..., the observed
- *            cumulative histogram read from its transposed copy (coalesced);
+ *            cumulative histogram read from its column-major copy (coalesced);
  *   k_distance (taller histograms, 1024 threads): the same in blocks of
- *            256 rows, with the column carry in a register.
+ *            256 rows (tile row pitch 33 words), with the column carry in a
+ *            register.
  * Warp w / lane l therefore own exactly the columns and rows they own in the
  * reference launch, so the per-lane sums, the shfl_down trees of reduce0
  * (:69-78) and the final per-warp tree reproduce the reference's float
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(1024, 1) k_distance(DistArgs a)
                         colcarry = __shfl_sync(0xFFFFFFFFu, s, 31);
                         if (valid) {
                             const uint32_t r = r0 + rr;
-                            const uint32_t ref = __ldg(refT + (uint64_t)col * R + r);
+                            const uint32_t ref = __ldg(refT + pcs_sat_t_index(r, col, R, B));
                             const float dd = __fsub_rn(__uint2float_rn(s), __uint2float_rn(ref));
                             a2 = __fadd_rn(a2, __fmul_rn(dd, dd));
                             if (F64) {
@@ -202,51 +202,66 @@ __global__ void __launch_bounds__(1024, 1) k_distance(DistArgs a)
     }
 }
 
-__device__ __forceinline__ uint32_t pick4_(const uint4& v, uint32_t i)
-{
-    return i == 0u ? v.x : (i == 1u ? v.y : (i == 2u ? v.z : v.w));
-}
-
 /* Strip kernel: 16 warps, full-height strips of 32 DE columns, a persistent
  * CTA walking the (proposal, strip) sequence blockIdx.x, blockIdx.x + grid,
  * ... strip by strip.
  *
- * Copy: warp w owns a contiguous segment of ceil(R/16) rows, lane i the
- * rows rb+i, rb+i+32, ... of it.  A row's 32 cells (128 bytes) move with
- * one bulk copy (cp.async.bulk, the TMA unit) completing on the tile's
- * mbarrier, when source, destination and size are 16-byte aligned (B a
- * multiple of 4 and an aligned histogram; every copy is checked before it
- * is issued); cells past B are zero-filled with plain stores.  Other rows
- * take 4-byte cp.async per cell (any B, any offset).  Every thread arrives
- * on the tile's mbarrier once per fill with the bytes of its bulk copies,
+ * Tile: rows of 32 cells (128 bytes) whose 16-byte chunks are permuted by
+ * XOR with (row mod 8) -- the TMA 128-byte swizzle -- so row-wise 128-bit
+ * accesses by lanes on consecutive rows, and column-wise accesses, are free
+ * of bank conflicts; 1024-byte aligned; rows up to the next multiple of 32.
+ * Copy: with a tensor map for the job (B x R x histograms, boxes of 32 x 32
+ * cells), one thread issues ceil(R/32) box copies (cp.async.bulk.tensor, the
+ * TMA unit) completing on the tile's mbarrier; rows past R and columns past
+ * B are outside the tensor and arrive as zeros.  Without one (B not a
+ * multiple of 4, R or B below 32, callers without maps), every lane copies
+ * its cells with 4-byte cp.async into the swizzled positions, zero-filling
+ * past R and B.  Every thread arrives on the tile's mbarrier once per fill,
  * so a waiter passes only when all copies of the strip have landed; the
  * wait is bounded (error bit 0x80 and a clean exit when it runs out).  With
  * two tiles (db) the copies of the next strip -- or of the next proposal's
  * first strip -- are in flight while the current strip is computed; with
  * one tile (tall histograms) the copies of a strip are issued together.
- * Phase A1: each lane sums column c0+l of its warp's segment (column totals
- * of the segment) and writes zeros back to the histogram, as K_distance
- * does.
- * Phase A2: lane l runs down column c0+l of the segment from the totals of
- * the segments above (column prefix), then lane j runs across row rb+j from
- * the row's carry of the strips to its left (row prefix, 128-bit shared
- * loads and stores): the tile holds the 2-D prefix sums after per-lane
- * chains through shared memory, no shuffles.
- * Phase B: warp w reads two columns of the strip, c0+w for logical warp w
- * and c0+w+16 for logical warp w+16 of the reference's 32x32 launch, so
- * every lane keeps the reference's per-lane sums in two accumulators; the
- * observed cumulative histogram of four 32-row groups is requested at once.
+ * Rows are split into 16 warp segments of a multiple of 8 rows (the
+ * segments reach the next multiple of 8 past R; those rows hold zeros), so
+ * a lane's swizzled column offset within each group of 8 rows is fixed.
+ * Phase A1: lane l runs down column c0+l of its warp's segment (column
+ * prefix within the segment, in place) and keeps the segment's column total;
+ * the strip is zeroed in the histogram, as K_distance does, by box stores
+ * of a zero box (one thread), or by the lanes cell by cell without a map.
+ * Phase A2: lane l adds the totals of the segments above (the column carry
+ * into the segment) and a warp scan turns the 32 carries into their prefix
+ * across the strip; lane j then runs across row rb+j from the row's carry
+ * of the strips to its left (128-bit shared loads and stores), adding the
+ * scanned column carry: the tile holds the 2-D prefix sums.
+ * Phase B: warp w reads columns c0+2w and c0+2w+1 -- logical warps 2w and
+ * 2w+1 of the reference's 32x32 launch -- with one 8-byte shared load per
+ * row, and the observed cumulative histogram of the same two columns with
+ * one coalesced 8-byte load per row (pair-interleaved copy), so every lane
+ * keeps the reference's per-lane sums in two accumulators.  When every
+ * cumulative count of the strip and of the observed histogram is below
+ * 2^22 (the largest is the last row's last cell: prefix sums of counts
+ * are monotone), float(s) - float(o) is the exact integer s - o, and it is
+ * formed as the float whose bits are 0x4B400000 + s - o (1.5 * 2^23 + s - o,
+ * exact in [2^23, 2^24)) minus 1.5 * 2^23: the same value the reference's
+ * two conversions and subtraction give, in two instructions.
  * SSD: also accumulate the exact integer sum of squares (128-bit per lane);
- * the PMC rounds do not ask for it, the parity entry point does.
- * Tile rows are 36 words (144 bytes): 16-byte aligned for the bulk copies,
- * and with 128-bit shared accesses (row pass, and the 16-byte chunk holding
- * a column in phase B) eight consecutive rows fall in eight different
- * bank groups, so both passes are free of bank conflicts.  R x 36 words per
- * tile: two tiles and two CTAs per SM up to ~385 rows. */
+ * the PMC rounds do not ask for it, the parity entry point does. */
 const uint32_t kStripThreads = 512;
-const int kStripRefGroups = 4;
-const uint32_t kSPitch = 36;                 /* strip tile row pitch (words) */
-const uint32_t kMbarWaitLimit = 1u << 22;    /* try_wait rounds before a wait is given up */
+const uint32_t kBox = 32;                     /* rows and columns of a tensor-map box */
+const uint32_t kBoxBytes = kBox * kBox * 4u;  /* 4096 */
+const uint32_t kMbarWaitLimit = 1u << 22;     /* try_wait rounds before a wait is given up */
+const uint32_t kExactBelow = 1u << 22;        /* cumulative counts below this take the integer difference */
+
+__host__ __device__ __forceinline__ uint32_t strip_cap_rows(uint32_t max_rows) { return (max_rows + 31u) & ~31u; }
+
+__device__ __forceinline__ uint32_t round8_(uint32_t x) { return (x + 7u) & ~7u; }
+
+/* word of (row r, column c) in a swizzled strip tile */
+__device__ __forceinline__ uint32_t sw_(uint32_t r, uint32_t c)
+{
+    return (r << 5) | ((((c >> 2) ^ (r & 7u)) << 2) | (c & 3u));
+}
 
 __device__ __forceinline__ uint32_t smem_u32_(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -282,16 +297,38 @@ __device__ __forceinline__ bool mbar_wait_(uint64_t* m, uint32_t parity)
     return false;
 }
 
-__device__ __forceinline__ void bulk_copy_(void* dst, const void* src, uint32_t bytes, uint64_t* m)
+/* the tensor map as written through global memory, for this thread's box copies */
+__device__ __forceinline__ void tmap_acquire_(const TmapDev* map)
 {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                     smem_u32_(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32_(m))
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(map) : "memory");
+}
+
+/* box (x, y, z) of a 3-D tensor map -> shared memory, completing on an mbarrier */
+__device__ __forceinline__ void tma_load_3d_(uint32_t* dst, const TmapDev* map, uint32_t x, uint32_t y, uint32_t z,
+                                             uint64_t* m)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+            smem_u32_(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32_(m))
+        : "memory");
+}
+
+/* shared memory -> box (x, y, z) of a 3-D tensor map (cells outside the tensor are dropped) */
+__device__ __forceinline__ void tma_store_3d_(const TmapDev* map, uint32_t x, uint32_t y, uint32_t z, const uint32_t* src)
+{
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];\n" ::"l"(map),
+                 "r"(x), "r"(y), "r"(z), "r"(smem_u32_(src))
                  : "memory");
 }
 
+__device__ __forceinline__ void bulk_commit_() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+
+/* this thread's box stores have completed */
+__device__ __forceinline__ void bulk_wait_all_() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+
 /* orders this thread's earlier generic shared-memory accesses before later
- * async-proxy (bulk copy) writes to the same memory */
+ * async-proxy (tensor copy) accesses to the same memory */
 __device__ __forceinline__ void fence_proxy_async_() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
 __device__ __forceinline__ void cp_async4_(uint32_t* dst, const uint32_t* src, bool valid)
@@ -306,50 +343,109 @@ __device__ __forceinline__ void cp_async_commit_() { asm volatile("cp.async.comm
 template <int N>
 __device__ __forceinline__ void cp_async_wait_() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-__device__ __forceinline__ bool aligned16_(const void* p) { return ((uintptr_t)p & 15u) == 0u; }
+/* warp w's segment of rows: [rb, re), multiples of 8, up to round8(R) */
+struct Seg {
+    uint32_t rb, re;
+};
 
-/* This thread's copies of strip c0 of proposal p into tile T, and its one
- * arrival on the tile's mbarrier (with the bytes of its bulk copies). */
-__device__ __forceinline__ void strip_copy_(const DistArgs& a, uint32_t p, uint32_t c0, uint32_t* T, uint32_t w,
-                                            uint32_t l, uint64_t* mbar)
+__device__ __forceinline__ Seg seg_(uint32_t R, uint32_t w)
+{
+    const uint32_t R8 = round8_(R);
+    const uint32_t n = round8_((R8 + 15u) / 16u);
+    Seg s;
+    s.rb = min(R8, w * n);
+    s.re = min(R8, s.rb + n);
+    return s;
+}
+
+/* proposal p's tensor map and its index along the map, or null (cell-by-cell copies) */
+__device__ __forceinline__ const TmapDev* prop_tmap_(const DistArgs& a, uint32_t p, uint32_t job, uint32_t& z)
+{
+    z = 0u;
+    if (!a.tmaps) return nullptr;
+    const uint32_t depth = a.jobs[job].tmap_depth;
+    z = a.props[p].hist_z;
+    return (depth != 0u && z < depth) ? a.tmaps + job : nullptr;
+}
+
+/* This thread's part of filling tile T with strip c0 of proposal p, and its
+ * one arrival on the tile's mbarrier. */
+__device__ __forceinline__ void strip_fill_(const DistArgs& a, uint32_t p, uint32_t c0, uint32_t* T, uint32_t tid,
+                                            uint64_t* mbar)
 {
     const uint32_t job = a.props[p].job;
     const uint32_t R = a.jobs[job].R, B = a.jobs[job].B;
-    const bool ok = R <= a.max_rows;
-    const uint32_t* hist = a.hist + a.props[p].hist_off;
-    const uint32_t seg = (R + 15u) / 16u;
-    const uint32_t rb = ok ? min(R, w * seg) : 0u, re = ok ? min(R, rb + seg) : 0u;
-    const uint32_t n = B > c0 ? min(32u, B - c0) : 0u; /* cells of this strip in a row */
-    const bool bulk_shape = n > 0u && (n & 3u) == 0u;
-    uint32_t bytes = 0u;
-    if (bulk_shape)
-        for (uint32_t r = rb + l; r < re; r += 32u)
-            if (aligned16_(hist + (uint64_t)r * B + c0) && aligned16_(T + r * kSPitch)) bytes += 4u * n;
-    mbar_arrive_expect_tx_(mbar, bytes);
-    for (uint32_t r = rb + l; r < re; r += 32u) {
-        const uint32_t* src = hist + (uint64_t)r * B + c0;
-        uint32_t* dst = T + r * kSPitch;
-        if (bulk_shape && aligned16_(src) && aligned16_(dst)) {
-            bulk_copy_(dst, src, 4u * n, mbar);
-            for (uint32_t c = n; c < 32u; ++c) dst[c] = 0u;
-        } else {
-            for (uint32_t c = 0; c < 32u; ++c) cp_async4_(dst + c, c < n ? src + c : hist, c < n);
-        }
+    if (R > a.max_rows) {
+        mbar_arrive_expect_tx_(mbar, 0u);
+        return;
     }
+    uint32_t z;
+    const TmapDev* map = prop_tmap_(a, p, job, z);
+    if (map) {
+        if (tid == 0u) {
+            const uint32_t nbox = (R + kBox - 1u) / kBox;
+            tmap_acquire_(map);
+            mbar_arrive_expect_tx_(mbar, nbox * kBoxBytes);
+            for (uint32_t b = 0; b < nbox; ++b) tma_load_3d_(T + b * kBox * 32u, map, c0, b * kBox, z, mbar);
+        } else {
+            mbar_arrive_expect_tx_(mbar, 0u);
+        }
+        return;
+    }
+    mbar_arrive_expect_tx_(mbar, 0u);
+    const uint32_t w = tid >> 5, l = tid & 31u;
+    const Seg sg = seg_(R, w);
+    const uint32_t* hist = a.hist + a.props[p].hist_off;
+    const uint32_t c = c0 + l, lc = l >> 2, lo = l & 3u;
+    for (uint32_t r8 = sg.rb; r8 < sg.re; r8 += 8u)
+#pragma unroll
+        for (uint32_t k = 0; k < 8u; ++k) {
+            const uint32_t r = r8 + k;
+            const bool v = r < R && c < B;
+            cp_async4_(T + (r << 5) + (((lc ^ k) << 2) | lo), v ? hist + (uint64_t)r * B + c : hist, v);
+        }
+}
+
+/* one distance term, general form: the reference's conversions, and on
+ * request the FP64 and exact integer sums and the prefix-sum output */
+template <bool F64, bool SSD>
+__device__ __forceinline__ void term_(uint32_t s, uint32_t o, float& a2, double& a2d, uint64_t& shi,
+                                      uint64_t& slo, uint32_t* cum, uint64_t at)
+{
+    const float dd = __fsub_rn(__uint2float_rn(s), __uint2float_rn(o));
+    a2 = __fadd_rn(a2, __fmul_rn(dd, dd));
+    if (SSD) {
+        const uint64_t ad = (s >= o) ? (uint64_t)(s - o) : (uint64_t)(o - s);
+        add128_(shi, slo, 0u, ad * ad);
+    }
+    if (F64) {
+        const double d64 = __dsub_rn((double)s, (double)o);
+        a2d = __dadd_rn(a2d, __dmul_rn(d64, d64));
+    }
+    if (cum) cum[at] = s;
+}
+
+/* float(s) - float(o) for s, o < 2^22 (exact integer difference) */
+__device__ __forceinline__ float exact_diff_(uint32_t s, uint32_t o)
+{
+    return __fsub_rn(__uint_as_float(0x4B400000u + s - o), 12582912.0f);
 }
 
 template <bool F64, bool SSD>
 __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t db)
 {
     extern __shared__ __align__(16) uint32_t s_mem[];
-    const uint32_t tile_words = a.max_rows * kSPitch;
-    /* 16-byte aligned tiles (the launch reserves 16 bytes for this) */
-    uint32_t* tiles = s_mem + ((16u - (smem_u32_(s_mem) & 15u)) & 15u) / 4u; /* [1 + db][max_rows][kSPitch] */
-    uint32_t* carry = s_mem + (1u + db) * tile_words;     /* [max_rows] */
+    const uint32_t tile_words = strip_cap_rows(a.max_rows) * 32u;
+    /* [1 + db][cap rows][32] tiles, 1024-byte aligned (the launch reserves
+     * 1024 bytes for this), a zero box, the row carries */
+    uint32_t* tiles = s_mem + ((1024u - (smem_u32_(s_mem) & 1023u)) & 1023u) / 4u;
+    uint32_t* zero = tiles + (1u + db) * tile_words;
+    uint32_t* carry = zero + kBox * kBox;
     __shared__ float s_tot[32];
     __shared__ double s_tot64[32];
     __shared__ uint64_t s_hi[32], s_lo[32];
-    __shared__ uint32_t s_col[16][32]; /* column totals of each warp's row segment */
+    __shared__ uint32_t s_col[16][32];             /* column totals of each warp's row segment */
+    __shared__ __align__(16) uint32_t s_K[16][32]; /* per segment: prefix across the strip of its column carries */
     __shared__ __align__(8) uint64_t s_mbar[2];
     __shared__ uint32_t s_abort;
 
@@ -364,11 +460,13 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
         mbar_init_fence_();
         s_abort = 0u;
     }
+    for (uint32_t i = tid; i < kBox * kBox; i += kStripThreads) zero[i] = 0u;
+    fence_proxy_async_(); /* the zero box, before box stores read it */
     __syncthreads();
 
     uint32_t c0 = 0, cur = 0, parity = 0u; /* parity bit b: the phase of tile b's next fill */
     uint32_t pending = 1u;                  /* bit b: tile b has a fill in flight */
-    strip_copy_(a, p, 0u, tiles, w, l, &s_mbar[0]);
+    strip_fill_(a, p, 0u, tiles, tid, &s_mbar[0]);
     cp_async_commit_();
 
     float acc0 = 0.0f, acc1 = 0.0f;
@@ -388,22 +486,22 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
         const bool has_next = pn < M;
         if (db) {
             if (has_next) {
-                strip_copy_(a, pn, cn, tiles + (cur ^ 1u) * tile_words, w, l, &s_mbar[cur ^ 1u]);
+                strip_fill_(a, pn, cn, tiles + (cur ^ 1u) * tile_words, tid, &s_mbar[cur ^ 1u]);
                 pending |= 1u << (cur ^ 1u);
             }
             cp_async_commit_();
-            cp_async_wait_<1>(); /* this thread's 4-byte copies of the current strip have landed */
+            cp_async_wait_<1>(); /* this thread's cell copies of the current strip have landed */
         } else {
             cp_async_wait_<0>();
         }
-        /* the current strip's bulk copies (all threads' arrivals and bytes) */
+        /* the current strip's box copies (all threads' arrivals and bytes) */
         if (!mbar_wait_(&s_mbar[cur], (parity >> cur) & 1u)) {
             atomicOr(a.err, PCS_ERRBIT_TIMEOUT);
             s_abort = 1u;
         }
         parity ^= 1u << cur;
         pending &= ~(1u << cur);
-        __syncwarp(); /* rows copied by other lanes of this warp (4-byte copies, zero fills) */
+        __syncwarp(); /* cells copied by other lanes of this warp */
         uint32_t* T = tiles + cur * tile_words;
         if (!ok) {
             if (tid == 0) {
@@ -414,94 +512,103 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
             const uint32_t* __restrict__ refT = a.jobs[job].ref_sat_t;
             uint32_t* hist = a.hist + hoff;
             uint32_t* cum = a.cum_out ? a.cum_out + hoff : nullptr;
-            const uint32_t seg = (R + 15u) / 16u;
-            const uint32_t rb = min(R, w * seg), re = min(R, rb + seg);
-            const uint32_t c = c0 + l;
-            const bool cin = c < B;
-            /* phase A1: this lane's cells -> column total, zeros written back */
-            uint32_t coltot = 0u;
-#pragma unroll 4
-            for (uint32_t r = rb; r < re; ++r) {
-                coltot += T[r * kSPitch + l];
-                if (cin) __stcs(hist + (uint64_t)r * B + c, 0u);
+            const Seg sg = seg_(R, w);
+            const uint32_t lc = l >> 2, lo = l & 3u;
+            /* phase A1: column prefix within the segment, segment totals */
+            uint32_t run = 0u;
+            for (uint32_t r8 = sg.rb; r8 < sg.re; r8 += 8u) {
+                uint32_t* t = T + (r8 << 5);
+#pragma unroll
+                for (uint32_t k = 0; k < 8u; ++k) {
+                    uint32_t* q = t + (k << 5) + (((lc ^ k) << 2) | lo);
+                    run += *q;
+                    *q = run;
+                }
             }
-            s_col[w][l] = coltot;
+            s_col[w][l] = run;
+            /* ... and the strip is zeroed in the histogram */
+            uint32_t z;
+            const TmapDev* map = prop_tmap_(a, p, job, z);
+            if (map) {
+                if (tid == 0u) {
+                    const uint32_t nbox = (R + kBox - 1u) / kBox;
+                    for (uint32_t b = 0; b < nbox; ++b) tma_store_3d_(map, c0, b * kBox, z, zero);
+                    bulk_commit_();
+                }
+            } else if (c0 + l < B) {
+                for (uint32_t r = sg.rb; r < min(sg.re, R); ++r) __stcs(hist + (uint64_t)r * B + c0 + l, 0u);
+            }
             __syncthreads();
             if (s_abort) break; /* a copy wait ran out (error word set) */
-            /* phase A2: column prefix down the segment, then row prefix across
-             * the strip: the tile holds the 2-D prefix sums */
-            uint32_t run = 0u;
-            for (uint32_t q = 0; q < w; ++q) run += s_col[q][l];
-#pragma unroll 4
-            for (uint32_t r = rb; r < re; ++r) {
-                run += T[r * kSPitch + l];
-                T[r * kSPitch + l] = run;
-            }
+            /* phase A2: column carry into the segment, scanned across the
+             * strip; then the row prefix from the left strips' row carry */
+            uint32_t cc = 0u;
+            for (uint32_t q = 0; q < w; ++q) cc += s_col[q][l];
+            s_K[w][l] = warp_scan_(cc, l);
             __syncwarp();
-            for (uint32_t r = rb + l; r < re; r += 32u) {
-                uint4* row4 = reinterpret_cast<uint4*>(T + r * kSPitch);
+            const uint4* K4 = reinterpret_cast<const uint4*>(s_K[w]);
+            for (uint32_t r = sg.rb + l; r < sg.re; r += 32u) {
+                uint4* row4 = reinterpret_cast<uint4*>(T + (r << 5));
+                const uint32_t m = r & 7u;
                 uint32_t acc = c0 ? carry[r] : 0u;
+                uint4 o = make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    uint4 v = row4[j];
-                    v.x += acc;
-                    v.y += v.x;
-                    v.z += v.y;
-                    v.w += v.z;
-                    acc = v.w;
-                    row4[j] = v;
+                for (uint32_t j = 0; j < 8u; ++j) {
+                    const uint4 v = row4[j ^ m];
+                    const uint4 k = K4[j];
+                    acc += v.x;
+                    o.x = acc + k.x;
+                    acc += v.y;
+                    o.y = acc + k.y;
+                    acc += v.z;
+                    o.z = acc + k.z;
+                    acc += v.w;
+                    o.w = acc + k.w;
+                    row4[j ^ m] = o;
                 }
-                carry[r] = acc;
+                carry[r] = o.w;
             }
             __syncthreads();
-            /* phase B: columns c0 + w and c0 + w + 16 */
-            const uint32_t colA = c0 + w, colB = c0 + w + 16u;
-            const bool inA = colA < B, inB = colB < B;
-            if (inA) {
+            /* phase B: columns c0 + 2w and c0 + 2w + 1; lane l reads rows
+             * l, l + 32, ..., all congruent to l mod 8, so its swizzled
+             * offset within a row is fixed */
+            const uint32_t colA = c0 + 2u * w;
+            if (colA < B) {
+                const bool inB = colA + 1u < B;
+                const uint32_t* Tl = T + ((((w >> 1) ^ (l & 7u)) << 2) | ((2u * w) & 3u));
+                const uint32_t* refc = refT + (uint64_t)colA * R; /* this column pair (or lone last column) */
                 float a2A = 0.0f, a2B = 0.0f;
                 double a2dA = 0.0, a2dB = 0.0;
-                for (uint32_t rg = 0; rg < R; rg += 32u * kStripRefGroups) {
-                    uint32_t refAv[kStripRefGroups], refBv[kStripRefGroups];
-#pragma unroll
-                    for (int g = 0; g < kStripRefGroups; ++g) {
-                        const uint32_t r = rg + 32u * (uint32_t)g + l;
-                        refAv[g] = r < R ? __ldg(refT + (uint64_t)colA * R + r) : 0u;
-                        refBv[g] = (r < R && inB) ? __ldg(refT + (uint64_t)colB * R + r) : 0u;
+                /* the largest cumulative counts: the strip's and the observed histogram's last cells */
+                const bool exact = !F64 && !SSD && !cum && T[sw_(R - 1u, 31u)] < kExactBelow &&
+                                   __ldg(refT + pcs_sat_t_index(R - 1u, B - 1u, R, B)) < kExactBelow;
+                if (exact && inB) {
+                    const uint2* ref2 = reinterpret_cast<const uint2*>(refc);
+#pragma unroll 4
+                    for (uint32_t r = l; r < R; r += 32u) {
+                        const uint2 s = *reinterpret_cast<const uint2*>(Tl + (r << 5));
+                        const uint2 o = __ldg(ref2 + r);
+                        const float dA = exact_diff_(s.x, o.x);
+                        const float dB = exact_diff_(s.y, o.y);
+                        a2A = __fadd_rn(a2A, __fmul_rn(dA, dA));
+                        a2B = __fadd_rn(a2B, __fmul_rn(dB, dB));
                     }
-#pragma unroll
-                    for (int g = 0; g < kStripRefGroups; ++g) {
-                        const uint32_t r = rg + 32u * (uint32_t)g + l;
-                        if (r < R) {
-                            const uint4 chA = reinterpret_cast<const uint4*>(T + r * kSPitch)[w >> 2];
-                            const uint32_t sA = pick4_(chA, w & 3u);
-                            const uint32_t refA = refAv[g];
-                            const float ddA = __fsub_rn(__uint2float_rn(sA), __uint2float_rn(refA));
-                            a2A = __fadd_rn(a2A, __fmul_rn(ddA, ddA));
-                            if (SSD) {
-                                const uint64_t adA = (sA >= refA) ? (uint64_t)(sA - refA) : (uint64_t)(refA - sA);
-                                add128_(shi, slo, 0u, adA * adA);
-                            }
-                            if (F64) {
-                                const double d64 = __dsub_rn((double)sA, (double)refA);
-                                a2dA = __dadd_rn(a2dA, __dmul_rn(d64, d64));
-                            }
-                            if (cum) cum[(uint64_t)r * B + colA] = sA;
-                            if (inB) {
-                                const uint4 chB = reinterpret_cast<const uint4*>(T + r * kSPitch)[(w >> 2) + 4u];
-                                const uint32_t sB = pick4_(chB, w & 3u);
-                                const uint32_t refB = refBv[g];
-                                const float ddB = __fsub_rn(__uint2float_rn(sB), __uint2float_rn(refB));
-                                a2B = __fadd_rn(a2B, __fmul_rn(ddB, ddB));
-                                if (SSD) {
-                                    const uint64_t adB = (sB >= refB) ? (uint64_t)(sB - refB) : (uint64_t)(refB - sB);
-                                    add128_(shi, slo, 0u, adB * adB);
-                                }
-                                if (F64) {
-                                    const double d64 = __dsub_rn((double)sB, (double)refB);
-                                    a2dB = __dadd_rn(a2dB, __dmul_rn(d64, d64));
-                                }
-                                if (cum) cum[(uint64_t)r * B + colB] = sB;
-                            }
+                } else if (exact) {
+#pragma unroll 4
+                    for (uint32_t r = l; r < R; r += 32u) {
+                        const float dA = exact_diff_(Tl[r << 5], __ldg(refc + r));
+                        a2A = __fadd_rn(a2A, __fmul_rn(dA, dA));
+                    }
+                } else {
+                    for (uint32_t r = l; r < R; r += 32u) {
+                        const uint64_t at = (uint64_t)r * B + colA;
+                        if (inB) {
+                            const uint2 s = *reinterpret_cast<const uint2*>(Tl + (r << 5));
+                            const uint2 o = __ldg(reinterpret_cast<const uint2*>(refc) + r);
+                            term_<F64, SSD>(s.x, o.x, a2A, a2dA, shi, slo, cum, at);
+                            term_<F64, SSD>(s.y, o.y, a2B, a2dB, shi, slo, cum, at + 1u);
+                        } else {
+                            term_<F64, SSD>(Tl[r << 5], __ldg(refc + r), a2A, a2dA, shi, slo, cum, at);
                         }
                     }
                 }
@@ -513,11 +620,11 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
                 }
             }
         }
-        fence_proxy_async_(); /* this tile's generic accesses before its next bulk fill */
+        fence_proxy_async_(); /* this tile's generic accesses before its next box fill */
         __syncthreads();      /* the tile is free for the copies issued next */
 
         if (ok && c0 + 32u >= B) {
-            /* last strip: reduce0 per logical warp (w and w + 16), then over
+            /* last strip: reduce0 per logical warp (2w and 2w + 1), then over
              * the 32 totals */
             const float ws0 = reduce0_(acc0), ws1 = reduce0_(acc1);
             double wd0 = 0.0, wd1 = 0.0;
@@ -533,14 +640,14 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
                 }
             }
             if (l == 0) {
-                s_tot[w] = ws0;
-                s_tot[w + 16] = ws1;
-                s_tot64[w] = wd0;
-                s_tot64[w + 16] = wd1;
-                s_hi[w] = shi;
-                s_lo[w] = slo;
-                s_hi[w + 16] = 0u;
-                s_lo[w + 16] = 0u;
+                s_tot[2u * w] = ws0;
+                s_tot[2u * w + 1u] = ws1;
+                s_tot64[2u * w] = wd0;
+                s_tot64[2u * w + 1u] = wd1;
+                s_hi[2u * w] = shi;
+                s_lo[2u * w] = slo;
+                s_hi[2u * w + 1u] = 0u;
+                s_lo[2u * w + 1u] = 0u;
             }
             __syncthreads();
             if (w == 0) {
@@ -571,7 +678,7 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
         }
         if (!has_next) break;
         if (!db) {
-            strip_copy_(a, pn, cn, tiles, w, l, &s_mbar[0]);
+            strip_fill_(a, pn, cn, tiles, tid, &s_mbar[0]);
             pending |= 1u;
             cp_async_commit_();
         } else {
@@ -584,14 +691,16 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
     /* after a given-up wait: let the fills still in flight land (bounded) */
     for (uint32_t b = 0; b < 2u; ++b)
         if ((pending >> b) & 1u) mbar_wait_(&s_mbar[b], (parity >> b) & 1u);
+    bulk_wait_all_(); /* the zero box stores have read the zero box before the CTA's shared memory goes */
 }
 
 static const size_t kStripSmemMax = 220u * 1024u;
 
-/* one or two tiles + carry + 16 bytes to align the tiles */
+/* 1024 bytes to align the tiles, one or two tiles, the zero box, the row carries */
 static size_t strip_smem_bytes(uint32_t max_rows, bool db)
 {
-    return ((size_t)max_rows * (1u + (db ? 2u : 1u) * kSPitch)) * sizeof(uint32_t) + 16u;
+    const size_t rows = strip_cap_rows(max_rows);
+    return 1024u + (db ? 2u : 1u) * rows * 32u * sizeof(uint32_t) + kBoxBytes + rows * sizeof(uint32_t);
 }
 
 static bool use_strip(uint32_t max_rows) { return strip_smem_bytes(max_rows, false) <= kStripSmemMax; }

@@ -136,7 +136,7 @@ __global__ void k_round_plan(PmcArgs a)
         rd->job_hist_base[j] = 0u;
     }
     uint32_t base = 0;
-    uint64_t hbase = 0;
+    uint64_t hbase = 0, cells = 0;
     for (uint32_t o = 0; o < nj; ++o) {
         const uint32_t j = ord[o];
         const JobPmcDev& pm = a.pmc[j];
@@ -145,7 +145,11 @@ __global__ void k_round_plan(PmcArgs a)
         uint64_t room = rd->capacity - base;
         const uint64_t rb = (uint64_t)a.jobs[j].R * a.jobs[j].B;
         if (rb) {
-            uint64_t hroom = (rd->hist_cap - hbase) / rb;
+            /* each job's histograms start at a multiple of R x B words, so
+             * one tensor map (B x R x histograms over the whole area) reaches
+             * every histogram of the job */
+            hbase = (hbase + rb - 1u) / rb * rb;
+            const uint64_t hroom = hbase < rd->hist_cap ? (rd->hist_cap - hbase) / rb : 0u;
             if (hroom < room) room = hroom;
         }
         uint64_t cnt = want < room ? want : room;
@@ -156,12 +160,13 @@ __global__ void k_round_plan(PmcArgs a)
         rd->job_hist_base[j] = hbase;
         base += (uint32_t)cnt;
         hbase += cnt * rb;
+        cells += cnt * rb;
     }
     rd->n_props = base;
     rd->n_items = 0u;
     rd->queue_head = 0u;
     rd->round_steps = 0ull;
-    rd->round_cells = hbase;
+    rd->round_cells = cells;
 }
 
 /* ----------------------------------------------------------------------- */
@@ -271,7 +276,7 @@ __global__ void __launch_bounds__(32 * kProposeWarps) k_propose(PmcArgs a)
     pd.slot = slot;
     pd.trial = trial;
     pd.gen = gen;
-    pd.quirk_full_az = 0u;
+    pd.hist_z = 0u;
     const double lambda = pcs_assemble_args(pm, th, ca, gen, pd);
     if (lane == 0u) {
         double* out = a.theta_prop + (uint64_t)q * PCS_MAX_P;
@@ -308,6 +313,8 @@ __global__ void __launch_bounds__(32 * kProposeWarps) k_propose(PmcArgs a)
     pd.total_particles = (uint32_t)min(total, (uint64_t)0xFFFFFFFFu);
     pd.counts_off = coff;
     pd.hist_off = rd->job_hist_base[j] + (uint64_t)local * ((uint64_t)jd.R * jd.B);
+    /* the job's histograms start at a multiple of R x B words (k_round_plan) */
+    pd.hist_z = (uint32_t)(pd.hist_off / max(1ull, (unsigned long long)jd.R * jd.B));
     pd.item_count = (pd.total_particles + rd->chunk - 1u) / rd->chunk;
     pd.item_begin = 0u;
     a.props[q] = pd;
@@ -883,7 +890,8 @@ __global__ void k_observed_bin_julia(const uint32_t* K, const double* DE, size_t
     }
 }
 
-/* column-wise then row-wise partial sums; also writes the transpose */
+/* column-wise then row-wise partial sums; also writes the column-major copy
+ * (pairs of columns interleaved, pcs_sat_t_index) */
 __global__ void k_observed_cols(uint32_t rows, uint32_t bins, uint32_t* sat)
 {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -903,7 +911,7 @@ __global__ void k_observed_rows(uint32_t rows, uint32_t bins, uint32_t* sat, uin
     for (uint32_t c = 0; c < bins; ++c) {
         acc += sat[(uint64_t)r * bins + c];
         sat[(uint64_t)r * bins + c] = acc;
-        if (sat_t) sat_t[(uint64_t)c * rows + r] = acc;
+        if (sat_t) sat_t[pcs_sat_t_index(r, c, rows, bins)] = acc;
     }
 }
 

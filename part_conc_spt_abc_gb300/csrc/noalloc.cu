@@ -3,7 +3,7 @@
  * for callers that cannot allocate device memory.
  *
  * pcs_scan_distance stages its inputs and its working buffers (the observed
- * cumulative histogram transposed for coalesced column sweeps, one
+ * cumulative histogram's column-major copy for coalesced column sweeps, one
  * descriptor per histogram, a proposal counter) in memory it allocates per
  * call.  Some callers cannot let a library call cudaMalloc: a host
  * framework whose caching allocator owns all device memory and must not be
@@ -14,7 +14,7 @@
  * allocates nothing.
  *
  * Limits: rows * bins <= PCS_NOALLOC_MAX_CELLS (1,048,576 cells, 4 MiB of
- * transposed histogram) and count <= PCS_NOALLOC_MAX_COUNT (4096 histograms);
+ * column-major histogram copy) and count <= PCS_NOALLOC_MAX_COUNT (4096 histograms);
  * larger requests are rejected with PCS_ERR_INVALID_ARGUMENT.  The array
  * (about 4.7 MiB) is reserved on every GPU that loads the library, until the
  * process exits.
@@ -61,7 +61,8 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 /* Fills the scratch for one call: job descriptor, one descriptor per
  * histogram (consecutive R x B blocks of the caller's buffer), the proposal
- * count, a cleared error word, and the transposed observed histogram. */
+ * count, a cleared error word, and the observed histogram's column-major
+ * copy (pairs of columns interleaved, pcs_sat_t_index). */
 __global__ void k_noalloc_setup(const uint32_t* __restrict__ ref_sat, uint32_t rows, uint32_t bins,
                                 uint32_t count)
 {
@@ -90,7 +91,7 @@ __global__ void k_noalloc_setup(const uint32_t* __restrict__ ref_sat, uint32_t r
     }
     for (uint64_t i = tid; i < cells; i += stride) {
         const uint64_t r = i / bins, b = i % bins;
-        ref_t[b * rows + r] = ref_sat[i];
+        ref_t[pcs_sat_t_index((uint32_t)r, (uint32_t)b, rows, bins)] = ref_sat[i];
     }
 }
 

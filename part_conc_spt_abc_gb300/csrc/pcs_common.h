@@ -4,7 +4,8 @@
  *
  * Layout in HBM (one GPU, everything device-resident for the life of a job):
  *   per job        JobDev descriptor, observed cumulative histogram (R x B,
- *                  row-major) and its transpose (B x R), frame counts [V],
+ *                  row-major) and its column-major copy with the columns
+ *                  interleaved in pairs (pcs_sat_t_index), frame counts [V],
  *                  population theta [N x P] f64, weights/cumulative weights
  *                  [N] f64, distances [N] f64, perturbation factor [P x P] f64,
  *                  slot bookkeeping [N] u32.
@@ -225,11 +226,32 @@ struct JobDev {
     uint32_t model, C, Z, P;
     uint32_t seed_lo, seed_hi;
     uint32_t frames_max;
-    uint32_t pad0;
+    uint32_t tmap_depth;   /* histograms the job's tensor map spans (0: no tensor map) */
     const uint32_t* frames;     /* [V] */
     const uint32_t* ref_sat;    /* [R*B] observed cumulative histogram */
-    const uint32_t* ref_sat_t;  /* [B*R] transposed copy, for column sweeps */
+    const uint32_t* ref_sat_t;  /* [B*R] column-major copy, pairs interleaved (pcs_sat_t_index) */
 };
+
+/* A TMA tensor map (CUtensorMap: 128 bytes, 64-byte aligned), stored as
+ * plain words so device tables need no driver header.  The histogram map of
+ * a job is three-dimensional -- B columns, R rows, histograms -- over a
+ * histogram area whose proposals of that job start at multiples of R x B
+ * words. */
+struct alignas(64) TmapDev {
+    uint64_t w[16];
+};
+
+/* Cell (row r, column b) of the column-major observed histogram of R rows
+ * and B columns, with columns 2j and 2j+1 interleaved: pair j occupies words
+ * [2jR, 2jR + 2R) as (r, 2j), (r, 2j+1) for r = 0..R-1, so one 8-byte load
+ * per row serves two columns and 32 consecutive rows are one coalesced
+ * 256-byte request.  An odd B's last column stands alone at [(B-1)R, BR). */
+PCS_HD uint64_t pcs_sat_t_index(uint32_t r, uint32_t b, uint32_t R, uint32_t B)
+{
+    const uint64_t base = (uint64_t)(b & ~1u) * R;
+    if ((b | 1u) < B) return base + 2ull * r + (b & 1u);
+    return base + r;
+}
 
 /* Per-proposal forward-model arguments (the SimulateRun of one proposal,
  * detail/simulation_impl.inl:319-340) plus its place in the round. */
@@ -241,7 +263,7 @@ struct PropDev {
     uint32_t total_particles;
     uint32_t item_begin;   /* first work item */
     uint32_t item_count;
-    uint32_t quirk_full_az;/* unused by kernels; kept for layout */
+    uint32_t hist_z;       /* this histogram's index along its job's tensor map (hist_off / (R x B)) */
     uint64_t hist_off;     /* offset of this proposal's R x B histogram (u32 words) */
     uint64_t counts_off;   /* offset of this proposal's [V] particle counts and [V+1] prefix */
     float half_az[PCS_MAX_C];

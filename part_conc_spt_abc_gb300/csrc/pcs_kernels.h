@@ -68,8 +68,15 @@ struct DistArgs {
     uint64_t* ssd;              /* [M][2] nullable: exact integer sum (hi, lo) */
     uint32_t* err;
     uint32_t max_rows;          /* rows of the carry array in shared memory */
+    const TmapDev* tmaps;       /* nullable: per job (index of jobs), tensor maps over hist */
 };
 cudaError_t launch_distance(const DistArgs& a, uint32_t grid, cudaStream_t st);
+/* Host: the tensor map of `depth` histograms of R x B u32 cells stored one
+ * after another from `base` (boxes of 32 columns x 32 rows, 128-byte
+ * swizzle).  False where the shape does not suit one (B a multiple of 4, R
+ * and B at least 32) or the driver refuses it; the kernel then copies cell
+ * by cell. */
+bool encode_hist_tmap(TmapDev* out, const uint32_t* base, uint32_t R, uint32_t B, uint64_t depth);
 size_t distance_smem_bytes(uint32_t max_rows);
 uint32_t distance_block_threads(uint32_t max_rows);
 int distance_ctas_per_sm(uint32_t max_rows);

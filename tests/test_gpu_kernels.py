@@ -105,6 +105,28 @@ def test_distance_batch_and_sizes(pcs, ctx, oracle, want_f64, want_ssd):
                 assert r["dist_f64"][q] == oracle.distance_kdist_f64(hist[q], ref), (R, B, q)
 
 
+@pytest.mark.parametrize("want_f64,want_ssd", [(False, False), (True, True)])
+def test_distance_large_counts(pcs, ctx, oracle, want_f64, want_ssd):
+    """Cumulative counts at and beyond 2^22 (where the strip kernel leaves
+    its integer-difference form for the reference's two conversions) and
+    beyond 2^24 (where those conversions round), in the simulated or only in
+    the observed histogram, with even and odd bin counts."""
+    rng = np.random.default_rng(11)
+    for R, B, lam_h, lam_r in [(301, 128, 200.0, 0.7), (301, 128, 0.7, 200.0), (257, 33, 2000.0, 2000.0),
+                               (120, 96, 400.0, 1.0)]:
+        n = 2
+        hist = rng.poisson(lam_h, (n, R, B)).astype(np.uint32)
+        ref = np.cumsum(np.cumsum(rng.poisson(lam_r, (R, B)), 0), 1).astype(np.uint32)
+        r = pcs.scan_distance(ctx, hist, ref, want_f64=want_f64, want_ssd=want_ssd)
+        for q in range(n):
+            d, _, ssd = oracle.distance_kdist(hist[q], ref)
+            assert r["dist_f32"][q].tobytes() == np.float32(d).tobytes(), (R, B, q)
+            if want_ssd:
+                assert r["ssd"][q] == ssd
+            if want_f64:
+                assert r["dist_f64"][q] == oracle.distance_kdist_f64(hist[q], ref), (R, B, q)
+
+
 def test_observed_sat_matches_oracle(pcs, ctx, oracle):
     rng = np.random.default_rng(5)
     R, B, ub = 1001, 1000, 5.0

@@ -238,3 +238,25 @@ def test_oracle_proposal_against_its_distributions(oracle):
         se = np.sqrt(lam / cs.size)
         assert abs(cs.mean() - lam) < 4 * se, (lam, cs.mean())
         assert abs(cs.var() / lam - 1) < 0.15, (lam, cs.var())
+
+
+@pytest.mark.parametrize("name", ["config0", "discrete_fixed_depth"])
+def test_posterior_fixture_observation(oracle, name):
+    """The committed posterior fixture: ten oracle seeds per case, each
+    posterior's 5-95% interval containing the synthetic truth, and the
+    observed histogram it was estimated from is the one the oracle's forward
+    model gives today (so the GPU side estimates from the same data)."""
+    import os
+    import sys
+    from conftest import GOLDEN
+    sys.path.insert(0, GOLDEN)
+    import posterior_cases as PC
+    z = np.load(os.path.join(GOLDEN, "posterior_cases.npz"))
+    case = PC.CASES[name]
+    np.testing.assert_array_equal(z[f"{name}__hist"], PC.observed_hist(oracle, case))
+    summ = z[f"{name}__summaries"]
+    assert summ.shape == (PC.SEEDS, len(PC.param_names(case)), 3)
+    free = PC.prior_ranges(case) > 0
+    truth = PC.truth_vector(case)
+    mean = summ.mean(0)
+    assert ((mean[free, 1] <= truth[free]) & (truth[free] <= mean[free, 2])).all(), (mean, truth)
