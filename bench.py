@@ -197,7 +197,9 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": f"{n} forward simulations per step at the true parameters"},
+        "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}"},
+        "run": {"step": f"{n} configuration-1 forward simulations at the true parameters (a bounded sample of the "
+                        "workload's forward-model work, timed on the host cores)"},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                          "sample": f"{n} config-1 forward simulations per step, Julia conventions, Float64"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -576,10 +578,12 @@ def measure_config(args, P, cfg, steps, warmup, rank, world, local, e2e=True):
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": steps, "warmup": warmup, "ms_per_step": ms_max / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload, "step": step_def, "parallelism": f"replicas x{world}",
-                   "l2": l2_note, "tuning": tune,
-                   "timed_region": {"steps": steps, "generations_ended": int(ks.generations),
-                                    "jobs_ended": jobs_ended, "generation_cap": GENERATIONS[cfg]}},
+        # the workload alone (the reference arm prints the same object);
+        # what this run chose and saw is under "run"
+        "config": {"workload": workload, "parallelism": f"replicas x{world}"},
+        "run": {"step": step_def, "l2": l2_note, "tuning": tune,
+                "timed_region": {"steps": steps, "generations_ended": int(ks.generations),
+                                 "jobs_ended": jobs_ended, "generation_cap": GENERATIONS[cfg]}},
         "proposals_per_s": props_all / (ms_max / 1e3),
         "accepted_per_s": acc_all / (ms_max / 1e3),
         "e2e": ({"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
@@ -678,8 +682,8 @@ def main():
                                                           "accepted_per_s", "roofline", "roofline_distance",
                                                           "kernel_ms", "clocks") if k in x}
             line[f"config{extra}"]["workload"] = x["config"]["workload"]
-            line[f"config{extra}"]["step"] = x["config"]["step"]
-            line[f"config{extra}"]["tuning"] = x["config"]["tuning"]
+            line[f"config{extra}"]["step"] = x["run"]["step"]
+            line[f"config{extra}"]["tuning"] = x["run"]["tuning"]
         line["pmc_pop4096"] = pmc_at_pop4096(P, local)
         # the serving stream and the served / plain comparison (spec target)
         line["serve"] = serve_section(args, P, local)
