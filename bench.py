@@ -40,19 +40,25 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Algorithmic thread-operations of the forward model, from the algorithm
-# (Philox4x32-10 call 80, Box-Muller pair 14):
-#   per-step walk, per particle-step: Philox 0.75 calls (60) + Box-Muller 1.5
-#     pairs (21) + walk, wrap, detection, DE (32) = 113;
+# Algorithmic thread-operations of the forward model, counted from the
+# algorithm (not from the compiled code): a uniform costs 22 (a quarter of a
+# Philox4x32-10 call at ~80 integer ops, plus ~2 to convert), a Box-Muller
+# pair 12 (log, sqrt, sincos, three multiplies), a full step of the walk 21
+# (position 3, wrap 9, detection 5, DE 4):
+#   per-step walk, per particle-step: 3 uniforms (66) + 1.5 pairs (18) + the
+#     step (21) = 105;
 #   slab-split walk, per particle-step of the z pass: per group of four steps
-#     Philox 1.5 calls (120) + Box-Muller 3 pairs (42) + four z steps (20) +
-#     summed x, y (10) = 192, i.e. 48 per step;
-#   slab-split walk, per task (a group walked in x, y): Philox 2 calls (160) +
-#     Box-Muller 4 pairs (56) + bridge means (12) + four x, y steps with
-#     detection and DE (72) + track bookkeeping (12) = 312.
-OPS_PER_STEP = 113
-OPS_SPLIT_STEP = 48
-OPS_SPLIT_TASK = 312
+#     6 uniforms (132) + 3 pairs (36) + four z steps (20) + summed x, y (10) =
+#     198, i.e. 49.5 per step;
+#   slab-split walk, per task (a group walked in x, y): 8 uniforms (176) + 4
+#     pairs (48) + bridge means (12) + four x, y steps with detection and DE
+#     (72) + track bookkeeping (12) = 320.
+# The compiled per-step walk executes fewer thread instructions than its 105
+# (~73 on a configuration-1 round, ncu): wide multiplies and fused
+# multiply-adds do more than one of these operations each.
+OPS_PER_STEP = 105
+OPS_SPLIT_STEP = 49.5
+OPS_SPLIT_TASK = 320
 # bytes the distance kernel moves per histogram cell: read count, write zero,
 # read the observed cumulative histogram
 DIST_BYTES_PER_CELL = 12

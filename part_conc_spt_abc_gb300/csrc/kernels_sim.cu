@@ -54,17 +54,52 @@ __device__ __forceinline__ void wrap3_(float& x, float& y, float& z, float hx, f
     }
 }
 
-/* Box-Muller on two 32-bit words: u1 in (0,1], angle uniform on [-pi, pi). */
-__device__ __forceinline__ void box_muller_(uint32_t ra, uint32_t rb, float& n0, float& n1)
+/* The PTX approximate instructions in their flush-to-zero forms.  Box-Muller
+ * never gives them a subnormal operand (u >= 2^-33; -2 ln u is 0 or above
+ * 5e-8; the angle is 0 or above 1e-7 in magnitude), so they return what the
+ * non-flushing forms (__log2f, __sincosf in a build without -ftz) return,
+ * without the subnormal handling those carry: ~10% fewer instructions per
+ * particle-step for the same normals. */
+__device__ __forceinline__ float lg2_ftz_(float x)
+{
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float sqrt_ftz_(float x)
+{
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float sin_ftz_(float x)
+{
+    float y;
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float cos_ftz_(float x)
+{
+    float y;
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+/* Box-Muller on two 32-bit words: u1 in (0,1], angle uniform on [-pi, pi);
+ * both normals times `scale` (the walk passes its particle's step sd, so
+ * its steps take the normals as they are: one multiply per pair instead of
+ * one per coordinate). */
+__device__ __forceinline__ void box_muller_(uint32_t ra, uint32_t rb, float& n0, float& n1, float scale = 1.0f)
 {
     float u = __fmaf_rn(__uint2float_rn(ra), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
-    float x = -1.3862943611198906f * __log2f(u); /* -2 ln u */
-    float rad = x * rsqrtf(fmaxf(x, 1e-30f));
+    float x = -1.3862943611198906f * lg2_ftz_(u); /* -2 ln u */
+    float rad = scale * sqrt_ftz_(x);
     float t = __fmaf_rn(__uint2float_rn(rb), 1.4629180792671596e-09f, -3.14159265358979f);
-    float s, c;
-    __sincosf(t, &s, &c);
-    n0 = rad * s;
-    n1 = rad * c;
+    n0 = rad * sin_ftz_(t);
+    n1 = rad * cos_ftz_(t);
 }
 
 struct Walker {
@@ -119,15 +154,17 @@ __device__ __forceinline__ void record_(const ItemCtx& c, uint32_t* tile, uint32
 
 /* One frame of the walk.  CHECK: the frame may lie past the particle's
  * last one (s >= F) and is then skipped; full groups of four frames call it
- * without the test. */
-template <bool AGG, bool CHECK = true>
+ * without the test.  SCALED: the normals already carry the step sd (fresh
+ * Philox draws); replayed normals are unit normals, scaled here as the
+ * reference scales them. */
+template <bool AGG, bool CHECK = true, bool SCALED = false>
 __device__ __forceinline__ void step_(const ItemCtx& c, uint32_t* tile, Walker& w, uint32_t s,
                                       float n0, float n1, float n2)
 {
     if (CHECK && s >= w.F) return;
-    float dx = __fmul_rn(w.sd, n0);
-    float dy = __fmul_rn(w.sd, n1);
-    float dz = __fmul_rn(w.sd, n2);
+    float dx = SCALED ? n0 : __fmul_rn(w.sd, n0);
+    float dy = SCALED ? n1 : __fmul_rn(w.sd, n1);
+    float dz = SCALED ? n2 : __fmul_rn(w.sd, n2);
     w.x = __fadd_rn(w.x, dx);
     w.y = __fadd_rn(w.y, dy);
     w.z = __fadd_rn(w.z, dz);
@@ -264,7 +301,8 @@ __device__ __forceinline__ void init_walker_(const SimArgs& a, const ItemCtx& c,
 }
 
 /* The 12 normals of the group of frames s0 .. s0+3: Philox blocks
- * 2+3g .. 4+3g through Box-Muller, or the replayed normals (zeros past F). */
+ * 2+3g .. 4+3g through Box-Muller, times the particle's step sd; or the
+ * replayed unit normals (zeros past F). */
 template <bool REPLAY>
 __device__ __forceinline__ void group_normals_(const SimArgs& a, const Walker& q, uint32_t s0, float* nn)
 {
@@ -278,8 +316,8 @@ __device__ __forceinline__ void group_normals_(const SimArgs& a, const Walker& q
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
             pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 2u + 3u * g + (uint32_t)b));
-            box_muller_(r.x, r.y, nn[4 * b + 0], nn[4 * b + 1]);
-            box_muller_(r.z, r.w, nn[4 * b + 2], nn[4 * b + 3]);
+            box_muller_(r.x, r.y, nn[4 * b + 0], nn[4 * b + 1], q.sd);
+            box_muller_(r.z, r.w, nn[4 * b + 2], nn[4 * b + 3], q.sd);
         }
     }
 }
@@ -293,18 +331,18 @@ __device__ __forceinline__ void walk_single_(const SimArgs& a, const ItemCtx& c,
     for (; s0 + 3u < q.F; s0 += 4u) {
         float nn[12];
         group_normals_<REPLAY>(a, q, s0, nn);
-        step_<AGG, false>(c, tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
-        step_<AGG, false>(c, tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
-        step_<AGG, false>(c, tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
-        step_<AGG, false>(c, tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
+        step_<AGG, false, !REPLAY>(c, tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
+        step_<AGG, false, !REPLAY>(c, tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
+        step_<AGG, false, !REPLAY>(c, tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
+        step_<AGG, false, !REPLAY>(c, tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
     }
     if (s0 < q.F) {
         float nn[12];
         group_normals_<REPLAY>(a, q, s0, nn);
-        step_<AGG>(c, tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
-        step_<AGG>(c, tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
-        step_<AGG>(c, tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
-        step_<AGG>(c, tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
+        step_<AGG, true, !REPLAY>(c, tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
+        step_<AGG, true, !REPLAY>(c, tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
+        step_<AGG, true, !REPLAY>(c, tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
+        step_<AGG, true, !REPLAY>(c, tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
     }
 }
 
@@ -421,10 +459,10 @@ __global__ void __launch_bounds__(sim_max_block(PPT)) k_simulate(SimArgs a)
                     if (s0 >= q.F) continue;
                     float nn[12];
                     group_normals_<REPLAY>(a, q, s0, nn);
-                    step_<AGG>(c, s_tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
-                    step_<AGG>(c, s_tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
-                    step_<AGG>(c, s_tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
-                    step_<AGG>(c, s_tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
+                    step_<AGG, true, !REPLAY>(c, s_tile, q, s0 + 0u, nn[0], nn[1], nn[2]);
+                    step_<AGG, true, !REPLAY>(c, s_tile, q, s0 + 1u, nn[3], nn[4], nn[5]);
+                    step_<AGG, true, !REPLAY>(c, s_tile, q, s0 + 2u, nn[6], nn[7], nn[8]);
+                    step_<AGG, true, !REPLAY>(c, s_tile, q, s0 + 3u, nn[9], nn[10], nn[11]);
                 }
             }
 #pragma unroll

@@ -26,8 +26,12 @@ def test_peaks_and_roofline_constants():
     b = load_bench()
     peaks, src = b.measured_peaks()
     assert src in ("measured", "fallback") and peaks.get("hbm_gbs", 0) > 0
-    # 0.75 Philox calls x 80 + 1.5 Box-Muller pairs x 14 + 32 walk operations
-    assert b.OPS_PER_STEP == 0.75 * 80 + 1.5 * 14 + 32
+    # per particle-step: 3 uniforms x 22 + 1.5 Box-Muller pairs x 12 + a 21-op step
+    assert b.OPS_PER_STEP == 3 * 22 + 1.5 * 12 + 21
+    # slab-split walk: (6 uniforms + 3 pairs + four z steps + summed x, y) / 4 steps;
+    # a task: 8 uniforms + 4 pairs + bridge means + four x, y steps + bookkeeping
+    assert b.OPS_SPLIT_STEP == (6 * 22 + 3 * 12 + 20 + 10) / 4
+    assert b.OPS_SPLIT_TASK == 8 * 22 + 4 * 12 + 12 + 72 + 12
     assert b.DIST_BYTES_PER_CELL == 12
 
 
