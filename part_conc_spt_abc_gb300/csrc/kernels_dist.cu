@@ -484,16 +484,7 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
             cn = 0u;
         }
         const bool has_next = pn < M;
-        if (db) {
-            if (has_next) {
-                strip_fill_(a, pn, cn, tiles + (cur ^ 1u) * tile_words, tid, &s_mbar[cur ^ 1u]);
-                pending |= 1u << (cur ^ 1u);
-            }
-            cp_async_commit_();
-            cp_async_wait_<1>(); /* this thread's cell copies of the current strip have landed */
-        } else {
-            cp_async_wait_<0>();
-        }
+        cp_async_wait_<0>(); /* this thread's cell copies of the current strip have landed */
         /* the current strip's box copies (all threads' arrivals and bytes) */
         if (!mbar_wait_(&s_mbar[cur], (parity >> cur) & 1u)) {
             atomicOr(a.err, PCS_ERRBIT_TIMEOUT);
@@ -507,6 +498,13 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
             if (tid == 0) {
                 atomicOr(a.err, PCS_ERRBIT_ROWS);
                 a.dist_f32[p] = __int_as_float(0x7fc00000);
+            }
+            __syncthreads();
+            if (s_abort) break; /* a copy wait ran out (error word set) */
+            if (db && has_next) {
+                strip_fill_(a, pn, cn, tiles + (cur ^ 1u) * tile_words, tid, &s_mbar[cur ^ 1u]);
+                pending |= 1u << (cur ^ 1u);
+                cp_async_commit_();
             }
         } else {
             const uint32_t* __restrict__ refT = a.jobs[job].ref_sat_t;
@@ -540,6 +538,13 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
             }
             __syncthreads();
             if (s_abort) break; /* a copy wait ran out (error word set) */
+            /* every warp is past the previous strip, whose tile the next
+             * strip's copies now fill (with two tiles) */
+            if (db && has_next) {
+                strip_fill_(a, pn, cn, tiles + (cur ^ 1u) * tile_words, tid, &s_mbar[cur ^ 1u]);
+                pending |= 1u << (cur ^ 1u);
+                cp_async_commit_();
+            }
             /* phase A2: column carry into the segment, scanned across the
              * strip; then the row prefix from the left strips' row carry */
             uint32_t cc = 0u;
@@ -620,8 +625,10 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
                 }
             }
         }
-        fence_proxy_async_(); /* this tile's generic accesses before its next box fill */
-        __syncthreads();      /* the tile is free for the copies issued next */
+        /* this tile's generic accesses before its next box fill, which
+         * follows the next strip's first barrier (with one tile, the
+         * barrier before the refill below) */
+        fence_proxy_async_();
 
         if (ok && c0 + 32u >= B) {
             /* last strip: reduce0 per logical warp (2w and 2w + 1), then over
@@ -678,6 +685,7 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
         }
         if (!has_next) break;
         if (!db) {
+            __syncthreads(); /* the one tile is free */
             strip_fill_(a, pn, cn, tiles, tid, &s_mbar[0]);
             pending |= 1u;
             cp_async_commit_();
