@@ -86,6 +86,8 @@ void autotune(Ctx& c, const pcs_params& p, const pcs_observed& obs, pcs_tuning* 
         a.dist_f32 = c.rb.dist32.as<float>();
         a.dist_f64 = c.rb.dist64.as<double>();
         a.err = c.err.as<uint32_t>();
+        a.logfact = c.logfact.as<double>();
+        a.logfact_n = kLogFactEntries;
         PCS_CUDA(launch_round_plan(a, c.stream));
         PCS_CUDA(launch_propose(a, c.rb.capacity, c.stream));
         PCS_CUDA(launch_items(a, c.stream));

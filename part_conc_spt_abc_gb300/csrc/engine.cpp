@@ -407,6 +407,12 @@ Ctx::Ctx(int dev, int infl) : device(dev), inflight(infl > 0 ? infl : 1)
     sim_tasks.alloc(8);
     PCS_CUDA(cudaMemset(sim_tasks.p, 0, 8));
     PCS_CUDA(cudaMemset(err.p, 0, 16));
+    {
+        std::vector<double> lf(kLogFactEntries);
+        for (uint32_t k = 0; k < kLogFactEntries; ++k) lf[k] = std::lgamma((double)k + 1.0);
+        logfact.alloc(sizeof(double) * kLogFactEntries);
+        PCS_CUDA(cudaMemcpy(logfact.p, lf.data(), sizeof(double) * kLogFactEntries, cudaMemcpyHostToDevice));
+    }
     PCS_CUDA(cudaMallocHost((void**)&h_err, 16));
     PCS_CUDA(cudaMallocHost((void**)&h_status, sizeof(JobPmcDev) * kMaxRoundJobs));
     PCS_CUDA(cudaMallocHost((void**)&h_round, sizeof(RoundDev)));
@@ -549,6 +555,8 @@ void Ctx::enqueue_round()
     a.dist_f32 = rb.dist32.as<float>();
     a.dist_f64 = rb.dist64.as<double>();
     a.err = err.as<uint32_t>();
+    a.logfact = logfact.as<double>();
+    a.logfact_n = kLogFactEntries;
     a.use_f64_distance = 0u;
     for (Job* j : table)
         if (j && j->p.distance_double) a.use_f64_distance = 1u;

@@ -82,6 +82,7 @@ struct Ctx {
     Tuning tune;
     DevBuf err;              /* device error word */
     DevBuf sim_tasks;        /* slab-split task counter (u64, cumulative) */
+    DevBuf logfact;          /* [kLogFactEntries] log(k!) from the host's lgamma */
     uint64_t sim_tasks_base = 0;
     uint32_t* h_err = nullptr;
     RoundBufs rb;

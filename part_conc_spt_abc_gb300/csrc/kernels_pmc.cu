@@ -283,7 +283,9 @@ __global__ void __launch_bounds__(32 * kProposeWarps) k_propose(PmcArgs a)
         for (uint32_t p = 0; p < P; ++p) out[p] = th[p];
     }
 
-    const PoissonSetup ps = pcs_poisson_setup(lambda);
+    PoissonSetup ps = pcs_poisson_setup(lambda);
+    ps.logfact = a.logfact;
+    ps.logfact_n = a.logfact_n;
     const uint64_t coff = (uint64_t)q * (2u * rd->v_max + 1u);
     uint32_t* cnt = a.counts + coff;
     uint32_t* pre = cnt + jd.V;

@@ -159,7 +159,12 @@ struct PmcArgs {
     double* dist_f64;         /* [capacity] nullable */
     uint32_t* err;
     uint32_t use_f64_distance;
+    uint32_t logfact_n;       /* entries of logfact */
+    const double* logfact;    /* nullable: log(k!) for k < logfact_n, for the Poisson sampler */
 };
+
+/* entries of the device log-factorial table (covers 1e5 particles per video) */
+const uint32_t kLogFactEntries = 1u << 17;
 
 cudaError_t launch_round_plan(const PmcArgs& a, cudaStream_t st);
 cudaError_t launch_propose(const PmcArgs& a, uint32_t capacity, cudaStream_t st);

@@ -74,9 +74,15 @@ PCS_HD double pcs_reflect(double bis, double lo, double hi)
  * (W. Hoermann, "The transformed rejection method for generating Poisson
  * random variables", Insurance: Mathematics and Economics 12, 1993).  The
  * constants depend on lambda only, so a proposal computes them once for all
- * of its videos. */
+ * of its videos.  logfact (nullable): log(k!) for k < logfact_n, built on
+ * the host with lgamma, which the device then reads instead of evaluating
+ * lgamma in FP64 (on this GPU a long chain of low-rate FP64 operations on
+ * the proposal kernel's critical path); past the table, and on the host,
+ * lgamma itself. */
 struct PoissonSetup {
     double lam, explam, loglam, b, a, invalpha, vr, log_invalpha;
+    const double* logfact;
+    uint32_t logfact_n;
 };
 
 PCS_HD PoissonSetup pcs_poisson_setup(double lam)
@@ -84,6 +90,8 @@ PCS_HD PoissonSetup pcs_poisson_setup(double lam)
     PoissonSetup ps;
     ps.lam = lam;
     ps.explam = ps.loglam = ps.b = ps.a = ps.invalpha = ps.vr = ps.log_invalpha = 0.0;
+    ps.logfact = nullptr;
+    ps.logfact_n = 0u;
     if (!(lam > 0.0)) return ps;
     if (lam < 12.0) {
         ps.explam = exp(-lam);
@@ -125,8 +133,8 @@ PCS_HD uint32_t pcs_poisson_draw(const PoissonSetup& ps, uint32_t video, uint32_
         const double kf = floor((2.0 * a / us + b) * U + lam + 0.43);
         if (us >= 0.07 && V <= ps.vr) return (uint32_t)kf;
         if (kf < 0.0 || (us < 0.013 && V > us)) continue;
-        if (log(V) + ps.log_invalpha - log(a / (us * us) + b) <= -lam + kf * ps.loglam - lgamma(kf + 1.0))
-            return (uint32_t)kf;
+        const double lf = (ps.logfact && kf < (double)ps.logfact_n) ? ps.logfact[(uint32_t)kf] : lgamma(kf + 1.0);
+        if (log(V) + ps.log_invalpha - log(a / (us * us) + b) <= -lam + kf * ps.loglam - lf) return (uint32_t)kf;
     }
     return (uint32_t)floor(lam + 0.5);
 }
@@ -234,7 +242,7 @@ PCS_HD CompArgs pcs_comp_args(const JobPmcDev& pm, const double* th, uint32_t i)
 {
     const Layout L = pcs_layout(pm);
     CompArgs ca;
-    ca.powc = pow(10.0, th[L.c + i]);
+    ca.powc = exp10(th[L.c + i]); /* 10^x: one exponential, where pow(10, x) adds a logarithm */
     if (pm.model == PCS_DEV_MODEL_LOGNORMAL) {
         /* lognormal diameter (nm), mean mu and sd s: sigma_ln^2 = ln(1 + s^2 / mu^2) */
         const double mu = th[L.m + i], sdv = th[L.s + i];
