@@ -419,9 +419,10 @@ pcs_status pcs_debug_particle_stream(pcs_ctx* ctx, uint64_t seed, uint32_t slot,
 /* The proposals of the context's last batched round that belong to `job`
  * (checks of the proposal construction, src/gpu/detail/simulation_impl.inl
  * :256-347, which the reference builds on the host per proposal): for each,
- * its slot, trial, generation, particle total and float forward-model
- * arguments, its parameter vector theta [n][P] (sample layout [m | s
- * (lognormal) | log10c | az]) and its particle counts [n][V].  They are
+ * its slot, trial, generation, particle total, float forward-model
+ * arguments and the float distance the round's distance kernel gave it
+ * (K_distance's value), its parameter vector theta [n][P] (sample layout
+ * [m | s (lognormal) | log10c | az]) and its particle counts [n][V].  They are
  * valid until the next round; the job must still be in the round table (not
  * retired).  With props NULL only *n is written. */
 typedef struct pcs_debug_proposal {
@@ -430,6 +431,7 @@ typedef struct pcs_debug_proposal {
     float pre_comp_prob[PCS_MAX_COMPONENTS];
     float sd_scale[PCS_MAX_COMPONENTS];
     float sd_shape[PCS_MAX_COMPONENTS];
+    float distance;
 } pcs_debug_proposal;
 pcs_status pcs_debug_round_proposals(pcs_job* job, uint32_t cap, uint32_t* n, pcs_debug_proposal* props,
                                      double* theta, uint32_t* counts);

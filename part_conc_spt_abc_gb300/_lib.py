@@ -113,6 +113,7 @@ class DebugProposal(C.Structure):
         ("slot", C.c_uint32), ("trial", C.c_uint32), ("generation", C.c_uint32), ("total_particles", C.c_uint32),
         ("half_az", C.c_float * MAX_COMPONENTS), ("pre_comp_prob", C.c_float * MAX_COMPONENTS),
         ("sd_scale", C.c_float * MAX_COMPONENTS), ("sd_shape", C.c_float * MAX_COMPONENTS),
+        ("distance", C.c_float),
     ]
 
 

@@ -851,6 +851,8 @@ pcs_status pcs_debug_round_proposals(pcs_job* job, uint32_t cap, uint32_t* n, pc
                             cudaMemcpyDeviceToHost));
         PCS_CUDA(cudaMemcpy(cv.data(), c.rb.counts.as<uint32_t>() + base * stride, cv.size() * 4,
                             cudaMemcpyDeviceToHost));
+        std::vector<float> dv(cnt);
+        PCS_CUDA(cudaMemcpy(dv.data(), c.rb.dist32.as<float>() + base, cnt * sizeof(float), cudaMemcpyDeviceToHost));
         for (uint32_t i = 0; i < cnt; ++i) {
             const PropDev& q = pd[i];
             pcs_debug_proposal& o = props[i];
@@ -864,6 +866,7 @@ pcs_status pcs_debug_round_proposals(pcs_job* job, uint32_t cap, uint32_t* n, pc
                 o.sd_scale[k] = q.sd_scale[k];
                 o.sd_shape[k] = q.sd_shape[k];
             }
+            o.distance = dv[i];
             for (uint32_t p = 0; p < j.P; ++p) theta[(size_t)i * j.P + p] = th[(size_t)i * PCS_MAX_P + p];
             const uint64_t off = q.counts_off - (uint64_t)base * stride;
             for (uint32_t v = 0; v < j.V; ++v) counts[(size_t)i * j.V + v] = cv[off + v];

@@ -319,3 +319,54 @@ def test_kernel_stats_account_for_the_rounds(pcs, ctx):
     assert ks.generations == 3  # the prior pass and two generations
     assert ks.pmc_bytes == 3 * (2 * N * P * 8 + N * 8)
     assert ks.pmc_pair_flops == 2 * N * N * (6 * P + 7)
+
+
+def test_round_distances_equal_the_standalone_kernels(pcs, ctx, oracle):
+    """Every proposal of served rounds that mix histogram shapes -- two with
+    tensor maps (61 x 48, 46 x 64) and two copied cell by cell (91 x 37 and
+    121 x 130: B not a multiple of 4) -- carries the distance that the
+    standalone kernels give: its
+    histogram rebuilt from its Philox coordinates (simulate_hist) and scanned
+    against its job's observed cumulative histogram (scan_distance), bit for
+    bit, as the oracle's K_distance restatement gives on the rebuilt
+    histogram."""
+    import part_conc_spt_abc_gb300.workloads as W
+    shapes = [(60, 48), (90, 37), (45, 64), (120, 130)]
+    seeds = [300 + i for i in range(len(shapes))]
+    jobs = [small_input(pcs, seed=20 + i, C=1 + i % 2, pop=48, frames=f, de_bins=b)[0]
+            for i, (f, b) in enumerate(shapes)]
+    srv = pcs.Server(ctx)
+    sims = [pcs.make_simulation(ctx, inp, s) for inp, s in zip(jobs, seeds)]
+    refs = []
+    for inp in jobs:
+        R, B = int(inp.frames.max()) + 1, inp.params.de_bin_count
+        refs.append(pcs.observed_sat(ctx, inp.K, inp.DE, R, B, inp.params.ub_de))
+    for s in sims:
+        srv.submit(s)
+    checked = 0
+    try:
+        for _ in range(6):
+            if srv.step() == 0:
+                break
+            for inp, sim, seed, ref in zip(jobs, sims, seeds, refs):
+                if srv.finished(sim):
+                    continue
+                props, _, counts = sim.round_proposals()
+                C, Z = sim.info().component_count, sim.info().z_component_count
+                setup = W.forward_setup(inp.frames, inp.params.de_bin_count, C=C)
+                for q, pr in enumerate(props[:24]):
+                    run = pcs.ForwardRun(counts[q], np.array(pr.half_az[:Z], np.float32),
+                                         np.array(pr.pre_comp_prob[:C], np.float32),
+                                         np.array(pr.sd_scale[:C], np.float32), np.array(pr.sd_shape[:C], np.float32),
+                                         slot=pr.slot, trial=pr.trial, generation=pr.generation)
+                    hist = pcs.simulate_hist(ctx, setup, run, seed=seed)[0]
+                    d = pcs.scan_distance(ctx, hist, ref)["dist_f32"][0]
+                    assert np.float32(pr.distance).tobytes() == np.float32(d).tobytes(), \
+                        (inp.params.de_bin_count, pr.slot, pr.trial, pr.generation, pr.distance, d)
+                    dw, _, _ = oracle.distance_kdist(hist, ref)
+                    assert np.float32(dw).tobytes() == np.float32(d).tobytes()
+                    checked += 1
+    finally:
+        for s in sims:
+            s.close()
+    assert checked >= 4 * 24
