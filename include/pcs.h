@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define PCS_ABI_VERSION 3
+#define PCS_ABI_VERSION 4
 #define PCS_MAX_COMPONENTS 8
 
 typedef enum pcs_status {

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(pcs):
 
 def test_host_only_calls(pcs):
     L = pcs.lib()
-    assert L.pcs_abi_version() == 3
+    assert L.pcs_abi_version() == 4
     assert L.pcs_status_string(0) == b"ok"
     p = pcs.params_defaults()
     assert p.delta_gamma == 0.01 and p.reference_initial_gamma == 1 and p.quantile == 0.5
