@@ -115,8 +115,17 @@ def _theta(case, out):
     return np.concatenate(cols, axis=1)
 
 
+@pytest.mark.parametrize("walk", [2, 1], ids=["step", "split"])
 @pytest.mark.parametrize("name", ["config0", "discrete_fixed_depth"])
-def test_posterior_matches_oracle_fixture(pcs, ctx, name):
+def test_posterior_matches_oracle_fixture(pcs, ctx, name, walk):
+    ctx.set_tuning(walk=walk)
+    try:
+        _fixture_case(pcs, ctx, name)
+    finally:
+        ctx.set_tuning(walk=2)
+
+
+def _fixture_case(pcs, ctx, name):
     import sys
     from conftest import GOLDEN
     sys.path.insert(0, GOLDEN)
