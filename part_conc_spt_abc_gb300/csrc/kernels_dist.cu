@@ -220,8 +220,11 @@ __global__ void __launch_bounds__(1024, 1) k_distance(DistArgs a)
  * so a waiter passes only when all copies of the strip have landed; the
  * wait is bounded (error bit 0x80 and a clean exit when it runs out).  With
  * two tiles (db) the copies of the next strip -- or of the next proposal's
- * first strip -- are in flight while the current strip is computed; with
- * one tile (tall histograms) the copies of a strip are issued together.
+ * first strip -- are issued after the current strip's first barrier (every
+ * warp is then past the strip before, whose tile they fill) and are in
+ * flight while the current strip is computed: two CTA barriers per strip.
+ * With one tile (tall histograms) the copies of a strip are issued together
+ * after a third barrier.
  * Rows are split into 16 warp segments of a multiple of 8 rows (the
  * segments reach the next multiple of 8 past R; those rows hold zeros), so
  * a lane's swizzled column offset within each group of 8 rows is fixed.
