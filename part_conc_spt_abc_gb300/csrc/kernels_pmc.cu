@@ -349,16 +349,20 @@ __global__ void __launch_bounds__(1024) k_items(PmcArgs a)
         run += a.props[q].item_count;
     }
     const uint32_t total = s_part[blockDim.x - 1];
-    __syncthreads();
+    const uint32_t cap = rd->items_cap;
+    __syncthreads(); /* every proposal's item_begin is written */
     if (threadIdx.x == 0) {
-        if (total > rd->items_cap) atomicOr(a.err, PCS_ERRBIT_ITEMS);
-        rd->n_items = min(total, rd->items_cap);
+        if (total > cap) atomicOr(a.err, PCS_ERRBIT_ITEMS);
+        rd->n_items = min(total, cap);
         rd->queue_head = 0u;
     }
-    for (uint32_t q = b; q < e; ++q) {
+    /* the item -> proposal map: a warp per proposal, its lanes on
+     * consecutive items (coalesced stores) */
+    const uint32_t lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
+    for (uint32_t q = threadIdx.x >> 5; q < M; q += nw) {
         const uint32_t ib = a.props[q].item_begin, ic = a.props[q].item_count;
-        for (uint32_t i = 0; i < ic; ++i)
-            if (ib + i < rd->items_cap) a.item_prop[ib + i] = q;
+        for (uint32_t i = lane; i < ic; i += 32u)
+            if (ib + i < cap) a.item_prop[ib + i] = q;
     }
 }
 
