@@ -83,6 +83,7 @@ struct PoissonSetup {
     double lam, explam, loglam, b, a, invalpha, vr, log_invalpha;
     const double* logfact;
     uint32_t logfact_n;
+    float lamf, af, bf, vrf, loglamf, linvf; /* the same constants rounded to float (pcs_ptrs_filtered) */
 };
 
 PCS_HD PoissonSetup pcs_poisson_setup(double lam)
@@ -92,6 +93,7 @@ PCS_HD PoissonSetup pcs_poisson_setup(double lam)
     ps.explam = ps.loglam = ps.b = ps.a = ps.invalpha = ps.vr = ps.log_invalpha = 0.0;
     ps.logfact = nullptr;
     ps.logfact_n = 0u;
+    ps.lamf = ps.af = ps.bf = ps.vrf = ps.loglamf = ps.linvf = 0.0f;
     if (!(lam > 0.0)) return ps;
     if (lam < 12.0) {
         ps.explam = exp(-lam);
@@ -104,9 +106,119 @@ PCS_HD PoissonSetup pcs_poisson_setup(double lam)
     ps.invalpha = 1.1239 + 1.1328 / (ps.b - 3.4);
     ps.vr = 0.9277 - 3.6224 / (ps.b - 2.0);
     ps.log_invalpha = log(ps.invalpha);
+    ps.lamf = (float)lam;
+    ps.af = (float)ps.a;
+    ps.bf = (float)ps.b;
+    ps.vrf = (float)ps.vr;
+    ps.loglamf = (float)ps.loglam;
+    ps.linvf = (float)ps.log_invalpha;
     return ps;
 }
 
+/* Scale of the FP32 filter's error margins below: 1 in the library; the
+ * CPU tests build a copy with a small scale to show that their comparison
+ * with the FP64 iteration detects margins that are too narrow. */
+#ifndef PCS_PTRS_MARGIN
+#define PCS_PTRS_MARGIN 1.0f
+#endif
+
+/* One PTRS iteration in FP64 on the draw r: 1 accept (*k), 0 reject. */
+PCS_HD int pcs_ptrs_exact(const PoissonSetup& ps, const pcs_u4& r, uint32_t* k)
+{
+    const double lam = ps.lam, a = ps.a, b = ps.b;
+    const double U = pcs_u01_53(r.x, r.y) - 0.5;
+    const double V = pcs_u01_53(r.z, r.w);
+    const double us = 0.5 - fabs(U);
+    const double kf = floor((2.0 * a / us + b) * U + lam + 0.43);
+    if (us >= 0.07 && V <= ps.vr) {
+        *k = (uint32_t)kf;
+        return 1;
+    }
+    if (kf < 0.0 || (us < 0.013 && V > us)) return 0;
+    const double lf = (ps.logfact && kf < (double)ps.logfact_n) ? ps.logfact[(uint32_t)kf] : lgamma(kf + 1.0);
+    if (log(V) + ps.log_invalpha - log(a / (us * us) + b) <= -lam + kf * ps.loglam - lf) {
+        *k = (uint32_t)kf;
+        return 1;
+    }
+    return 0;
+}
+
+/* The same iteration decided in FP32 where that is certain: every test of
+ * pcs_ptrs_exact evaluated on the top 24 bits of its uniforms (U and V then
+ * differ from the FP64 ones by less than u = 2^-24) with a bound on the
+ * FP32 error, derived term by term below (u per rounding, the inputs'
+ * truncation, 1 ulp per logf); a test inside its bound, a small us, a V near
+ * 0 or a k past the log-factorial table leaves the iteration to
+ * pcs_ptrs_exact (-1).  Where it decides, its decision and k are the FP64
+ * iteration's: the counts do not change, most of the FP64 work does.
+ * On this GPU FP64 runs at a small fraction of the FP32 rate. */
+PCS_HD int pcs_ptrs_filtered(const PoissonSetup& ps, const pcs_u4& r, uint32_t* k)
+{
+    const float u = 5.9604645e-8f; /* 2^-24 */
+    if (!(ps.lamf <= 4.0e6f)) return -1; /* k exact in float with room */
+    const float Uf = (float)(r.x >> 8) * u - 0.5f; /* U - Uf in [0, u) */
+    const float Vf = (float)(r.z >> 8) * u;        /* V - Vf in [0, u) */
+    const float usf = 0.5f - fabsf(Uf);            /* |us - usf| < u */
+    const float m = 4.0e-7f; /* input truncation plus the constants' rounding to float */
+    /* us >= 0.07 and V <= vr */
+    const int A = usf > 0.07f + m ? 1 : (usf < 0.07f - m ? 0 : -1);
+    const int Bv = Vf < ps.vrf - m ? 1 : (Vf > ps.vrf + m ? 0 : -1);
+    const bool fast_no = A == 0 || Bv == 0;
+    if (!fast_no && (A < 0 || Bv < 0)) return -1;
+    /* us < 0.013 and V > us */
+    const int C1 = usf < 0.013f - m ? 1 : (usf > 0.013f + m ? 0 : -1);
+    const int C2 = Vf > usf + m ? 1 : (Vf < usf - m ? 0 : -1);
+    if (fast_no && C1 == 1 && C2 == 1) return 0;
+    /* k = floor((2a/us + b) U + lam + 0.43).  With ru = 1.01 u / usf above
+     * us's relative error, 2a/us is within (2u + ru)|t1|, and x within
+     * (u + ru/2)|t1| + u (0.5|b| + 1.5|t2| + 2|t3| + 2 lam + |x| + 0.43);
+     * the margin doubles that (and covers the FP64 evaluation's own
+     * rounding) */
+    if (usf < 0.005f) return -1;
+    const float ru = 1.01f * u / usf;
+    const float t1 = 2.0f * ps.af / usf;
+    const float t2 = t1 + ps.bf;
+    const float t3 = t2 * Uf;
+    const float xf = (t3 + ps.lamf) + 0.43f;
+    const float mx = PCS_PTRS_MARGIN * ((4.0f * u + 1.2f * ru) * fabsf(t1) +
+                                        u * (4.0f * (fabsf(ps.bf) + fabsf(t2) + fabsf(t3)) + 4.0f * ps.lamf +
+                                             4.0f * fabsf(xf) + 8.0f));
+    const float n = floorf(xf);
+    if (!(xf - n > mx && (n + 1.0f) - xf > mx)) return -1;
+    if (!fast_no) { /* A and Bv both 1 */
+        *k = (uint32_t)n;
+        return 1;
+    }
+    if (n < 0.0f) return 0;
+    if (C1 < 0 || C2 < 0) {
+        if (!(C1 == 0 || C2 == 0)) return -1;
+    }
+    /* log(V) + log_invalpha - log(a/us^2 + b) <= -lam + k loglam - log(k!) */
+    if (!ps.logfact || !(n < (float)ps.logfact_n) || Vf < 1.0e-6f) return -1;
+    const float lf = (float)ps.logfact[(uint32_t)n];
+    const float lV = logf(Vf);
+    const float l2 = logf(ps.af / (usf * usf) + ps.bf);
+    const float lhs = (lV + ps.linvf) - l2;
+    const float kl = n * ps.loglamf;
+    const float rhs = (kl - ps.lamf) - lf;
+    const float d = lhs - rhs;
+    /* error of lhs below u/V (V's truncation) + 3u|log V| + 2u|log_invalpha|
+     * + (4u + 2ru) (a/us^2 + b is positive, to that relative error) + 2u|l2|
+     * + u|lhs|; of rhs below 2u lam + 3u|k loglam| + u|log k!| + u|rhs|; of
+     * d, u|d| more.  The margin is at least that sum with room for its own
+     * rounding. */
+    const float ms = PCS_PTRS_MARGIN * 2.4f * ru + PCS_PTRS_MARGIN * u * (1.0f / Vf + 4.0f * fabsf(lV) + 3.0f * fabsf(ps.linvf) + 4.0f * fabsf(l2) +
+                                     2.0f * fabsf(lhs) + 16.0f + 4.0f * ps.lamf + 4.0f * fabsf(kl) +
+                                     2.0f * fabsf(lf) + 2.0f * fabsf(rhs) + 2.0f * fabsf(d));
+    if (d < -ms) {
+        *k = (uint32_t)n;
+        return 1;
+    }
+    if (d > ms) return 0;
+    return -1;
+}
+
+template <bool FILTER = true>
 PCS_HD uint32_t pcs_poisson_draw(const PoissonSetup& ps, uint32_t video, uint32_t slot, uint32_t gt, uint32_t k0,
                                  uint32_t k1)
 {
@@ -124,17 +236,12 @@ PCS_HD uint32_t pcs_poisson_draw(const PoissonSetup& ps, uint32_t video, uint32_
         }
         return k;
     }
-    const double a = ps.a, b = ps.b;
     for (uint32_t it = 0; it < 256u; ++it) {
         const pcs_u4 r = pcs_draw(video, pcs_ctr_tag(PCS_STREAM_POISSON, 1u + it), slot, gt, k0, k1);
-        const double U = pcs_u01_53(r.x, r.y) - 0.5;
-        const double V = pcs_u01_53(r.z, r.w);
-        const double us = 0.5 - fabs(U);
-        const double kf = floor((2.0 * a / us + b) * U + lam + 0.43);
-        if (us >= 0.07 && V <= ps.vr) return (uint32_t)kf;
-        if (kf < 0.0 || (us < 0.013 && V > us)) continue;
-        const double lf = (ps.logfact && kf < (double)ps.logfact_n) ? ps.logfact[(uint32_t)kf] : lgamma(kf + 1.0);
-        if (log(V) + ps.log_invalpha - log(a / (us * us) + b) <= -lam + kf * ps.loglam - lf) return (uint32_t)kf;
+        uint32_t kk = 0u;
+        int dec = FILTER ? pcs_ptrs_filtered(ps, r, &kk) : -1;
+        if (dec < 0) dec = pcs_ptrs_exact(ps, r, &kk);
+        if (dec > 0) return kk;
     }
     return (uint32_t)floor(lam + 0.5);
 }

@@ -7,7 +7,11 @@ fixed), and computing its constants once per proposal gives the same draws
 as computing them per draw; the Box-Muller pair is standard normal and
 uncorrelated; the reflection is the reference's displace_ (the oracle's
 restatement) wherever that terminates, and stays in the box beyond; the
-parent pick is std::lower_bound clamped to N - 1."""
+parent pick is std::lower_bound clamped to N - 1.  The PTRS iteration's
+FP32 filter decides exactly as the FP64 iteration wherever it decides (on
+Philox draws and on draws placed at the tests' thresholds), so the filtered
+sampler's draws equal the FP64 sampler's; a copy built with margins at 1%
+of the library's shows that the comparison finds narrow margins."""
 import ctypes as C
 import math
 import os
@@ -21,16 +25,19 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(ROOT, "part_conc_spt_abc_gb300", "csrc")
 
 
-@pytest.fixture(scope="module")
-def harness(tmp_path_factory):
+def build_harness(tmp_path_factory, defines=()):
     cxx = shutil.which("g++")
     cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
     if not cxx or not os.path.exists(os.path.join(cuda_inc, "cuda_runtime.h")):
         pytest.skip("g++ or the CUDA headers are missing")
     out = str(tmp_path_factory.mktemp("proposal") / "libproposal_pieces.so")
-    subprocess.check_call([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", CSRC, "-I", cuda_inc,
+    subprocess.check_call([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", *defines, "-I", CSRC, "-I", cuda_inc,
                            os.path.join(ROOT, "tests", "harness", "proposal_pieces.cpp"), "-o", out])
     lib = C.CDLL(out)
+    lib.ptrs_check.argtypes = [C.c_double, C.c_uint32, C.c_uint64, C.c_int, C.POINTER(C.c_uint64)]
+    lib.ptrs_check.restype = None
+    lib.poisson_filter_diffs.argtypes = [C.c_double, C.c_uint32, C.c_uint64]
+    lib.poisson_filter_diffs.restype = C.c_uint32
     lib.draw_poisson.argtypes = [C.c_double, C.c_uint32, C.c_uint64, C.POINTER(C.c_uint32)]
     lib.draw_poisson.restype = None
     lib.draw_poisson_one.argtypes = [C.c_double, C.c_uint32, C.c_uint32, C.c_uint64]
@@ -42,6 +49,17 @@ def harness(tmp_path_factory):
     lib.normals.argtypes = [C.c_uint32, C.c_uint64, C.POINTER(C.c_double)]
     lib.normals.restype = None
     return lib
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    return build_harness(tmp_path_factory)
+
+
+def ptrs_check(lib, lam, n, seed, with_table=1):
+    out = (C.c_uint64 * 4)()
+    lib.ptrs_check(lam, n, seed, with_table, out)
+    return dict(decided=out[0] / n, mismatches=int(out[1]), accepts=out[2] / n, filter_accepts=out[3] / n)
 
 
 def draws(lib, lam, n, seed):
@@ -126,3 +144,26 @@ def test_parent_pick_is_lower_bound(harness):
         for u in list(rng.random(200)) + [0.0, float(wcum[0]), float(wcum[-1])]:
             want = min(int(np.searchsorted(wcum, u, side="left")), N - 1)
             assert harness.pick(p, N, u) == want, (N, u)
+
+
+LAMS_PTRS = [12.0, 12.7, 55.5, 320.0, 1000.0, 4096.0, 25000.0, 1.0e5, 1.3e5, 1.0e6, 5.0e6]
+
+
+@pytest.mark.parametrize("lam", LAMS_PTRS)
+def test_ptrs_fp32_filter_decides_as_fp64(harness, lam):
+    n = 2_000_000
+    r = ptrs_check(harness, lam, n, seed=7)
+    assert r["mismatches"] == 0, r
+    if lam <= 1.0e5:
+        # the filter carries most iterations (a quarter of the draws sit at thresholds)
+        assert r["decided"] > 0.6, r
+    # the same without the log-factorial table: the slow test stays in FP64
+    r = ptrs_check(harness, lam, n // 4, seed=8, with_table=0)
+    assert r["mismatches"] == 0, r
+    assert harness.poisson_filter_diffs(lam, n // 4, 11) == 0
+
+
+def test_ptrs_check_finds_narrow_margins(tmp_path_factory):
+    weak = build_harness(tmp_path_factory, defines=("-DPCS_PTRS_MARGIN=0.01f",))
+    bad = sum(ptrs_check(weak, lam, 1_000_000, seed=7)["mismatches"] for lam in (320.0, 4096.0, 1.0e5))
+    assert bad > 0
