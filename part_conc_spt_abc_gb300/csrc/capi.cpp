@@ -747,7 +747,8 @@ pcs_status pcs_scan_distance(pcs_ctx* ctx, const uint32_t* hist, const uint32_t*
         d.err = c.err.as<uint32_t>();
         d.max_rows = rows;
         d.tmaps = d_map;
-        PCS_CUDA(launch_distance(d, std::min<uint32_t>(count, (uint32_t)(distance_ctas_per_sm(rows) * c.sm_count)), st));
+        const uint32_t cl = (d_cum || d_d64 || d_ssd) ? 0u : distance_cluster_size(rows, bins);
+        PCS_CUDA(launch_distance(d, std::min<uint32_t>(count, (uint32_t)(distance_ctas_per_sm(rows) * c.sm_count)), st, cl));
         if (cum_out) PCS_CUDA(cudaMemcpyAsync(cum_out, d_cum, count * RB * 4, cudaMemcpyDeviceToHost, st));
         PCS_CUDA(cudaMemcpyAsync(dist_f32, d_d32, count * 4, cudaMemcpyDeviceToHost, st));
         if (dist_f64) PCS_CUDA(cudaMemcpyAsync(dist_f64, d_d64, count * 8, cudaMemcpyDeviceToHost, st));

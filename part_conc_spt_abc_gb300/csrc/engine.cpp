@@ -601,8 +601,10 @@ void Ctx::enqueue_round()
     d.err = a.err;
     d.max_rows = rb.max_rows;
     d.tmaps = rb.tmaps.as<TmapDev>();
+    const uint32_t cl = d.dist_f64 ? 0u : distance_cluster_size(rb.max_rows, rb_max_b_);
     PCS_CUDA(cudaEventRecordWithFlags(ev_dist0, stream, cudaEventRecordExternal));
-    PCS_CUDA(launch_distance(d, std::min<uint32_t>(rb.capacity, (uint32_t)(distance_ctas_per_sm(rb.max_rows) * sm_count)), stream));
+    PCS_CUDA(launch_distance(d, std::min<uint32_t>(rb.capacity, (uint32_t)(distance_ctas_per_sm(rb.max_rows) * sm_count)),
+                             stream, cl));
     PCS_CUDA(cudaEventRecordWithFlags(ev_dist1, stream, cudaEventRecordExternal));
 
     PCS_CUDA(cudaEventRecordWithFlags(ev_pmc0, stream, cudaEventRecordExternal));

@@ -26,6 +26,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pcs_common.h"
 #include "pcs_kernels.h"
 
@@ -346,6 +348,45 @@ __device__ __forceinline__ void cp_async_commit_() { asm volatile("cp.async.comm
 template <int N>
 __device__ __forceinline__ void cp_async_wait_() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+/* thread-block cluster: this CTA's rank, the cluster's index and count */
+__device__ __forceinline__ uint32_t cluster_rank_()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t cluster_id_()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;\n" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t cluster_count_()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%nclusterid.x;\n" : "=r"(r));
+    return r;
+}
+
+/* every thread of every CTA of the cluster; shared-memory writes before it
+ * are visible to shared::cluster reads after it */
+__device__ __forceinline__ void cluster_sync_()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+/* the word at `p` (this CTA's shared memory) in the shared memory of the
+ * cluster's CTA `rank` */
+__device__ __forceinline__ uint32_t ld_cluster_(const void* p, uint32_t rank)
+{
+    uint32_t ra, v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(ra) : "r"(smem_u32_(p)), "r"(rank));
+    asm volatile("ld.shared::cluster.u32 %0, [%1];\n" : "=r"(v) : "r"(ra) : "memory");
+    return v;
+}
+
 /* warp w's segment of rows: [rb, re), multiples of 8, up to round8(R) */
 struct Seg {
     uint32_t rb, re;
@@ -432,6 +473,281 @@ __device__ __forceinline__ void term_(uint32_t s, uint32_t o, float& a2, double&
 __device__ __forceinline__ float exact_diff_(uint32_t s, uint32_t o)
 {
     return __fsub_rn(__uint_as_float(0x4B400000u + s - o), 12582912.0f);
+}
+
+/* Cluster mode (k_distance_cluster), for launches where walking each
+ * histogram's strips one after another in one CTA leaves SMs idle or takes
+ * long: few histograms, or tall ones.  A cluster
+ * of `cl` CTAs takes one histogram at a time, CTA k its strip k (columns
+ * 32k..32k+31; cl is at least the strips of every job).  Each CTA builds
+ * its strip's 2-D prefix sums as if the strip stood alone (row carry 0) and
+ * publishes the last column, P_k(r) = the cells of rows <= r in the strip;
+ * after a cluster barrier CTA k's row carry is sum_{j<k} P_j(r), read from
+ * the other CTAs' shared memory (integers, so the prefix sums are the strip
+ * walk's exactly).  Each CTA then forms its strip's per-lane sums for
+ * logical warps 2w, 2w+1 as the strip walk does and publishes them; after
+ * the next barrier CTA 0 adds each (logical warp, lane)'s strip sums in
+ * strip order -- the strip walk's per-lane accumulation, operation for
+ * operation -- and reduces them with the same trees: the same float, bit
+ * for bit.  One barrier per histogram: P and the per-lane sums alternate
+ * between two buffers, and CTA 0 reduces histogram i while the cluster
+ * computes histogram i + 1.  The next histogram's strip is copied in while
+ * the current one is computed (two tiles).  A copy wait that runs out ends
+ * the loop on every CTA of the cluster together (each reads all CTAs' flags
+ * after the barrier), so no CTA is left waiting at a cluster barrier. */
+__device__ __forceinline__ void cluster_fill_(const DistArgs& a, uint32_t p, uint32_t k, uint32_t cl, uint32_t* T,
+                                              uint32_t tid, uint64_t* mbar)
+{
+    const uint32_t ns = (a.jobs[a.props[p].job].B + 31u) / 32u;
+    if (k < ns && ns <= cl) strip_fill_(a, p, 32u * k, T, tid, mbar);
+    else mbar_arrive_expect_tx_(mbar, 0u);
+}
+
+/* CTA 0: histogram p's distance from every strip's per-lane sums */
+__device__ __forceinline__ void cluster_reduce_(const DistArgs& a, uint32_t p, uint32_t cl, const float* part,
+                                                float* s_tot)
+{
+    const uint32_t tid = threadIdx.x, w = tid >> 5, l = tid & 31u;
+    const uint32_t job = a.props[p].job;
+    const uint32_t B = a.jobs[job].B;
+    if (!(a.jobs[job].R <= a.max_rows && (B + 31u) / 32u <= cl)) {
+        if (tid == 0u) {
+            atomicOr(a.err, PCS_ERRBIT_ROWS);
+            a.dist_f32[p] = __int_as_float(0x7fc00000);
+        }
+        return;
+    }
+    const uint32_t ns = (B + 31u) / 32u;
+#pragma unroll
+    for (uint32_t h = 0; h < 2u; ++h) {
+        const uint32_t lw = 2u * w + h;
+        float acc = 0.0f;
+        for (uint32_t j = 0; j < ns; ++j)
+            if (32u * j + lw < B) acc = __fadd_rn(acc, __uint_as_float(ld_cluster_(part + lw * 32u + l, j)));
+        const float ws = reduce0_(acc);
+        if (l == 0u) s_tot[lw] = ws;
+    }
+    __syncthreads();
+    if (w == 0u) {
+        const float fin = reduce0_(s_tot[l]);
+        if (l == 0u) a.dist_f32[p] = fin;
+    }
+}
+
+__device__ __forceinline__ void strip_cluster_(const DistArgs& a, uint32_t db, uint32_t cl, uint32_t M,
+                                               uint32_t* tiles, uint32_t tile_words, const uint32_t* zero,
+                                               uint32_t* carry, uint32_t* P2, float* part2, float* s_tot,
+                                               uint32_t (*s_col)[32], uint32_t (*s_K)[32], uint64_t* s_mbar,
+                                               uint32_t* s_abort)
+{
+    const uint32_t tid = threadIdx.x;
+    const uint32_t w = tid >> 5, l = tid & 31u;
+    const uint32_t k = cluster_rank_(), ncl = cluster_count_();
+    const uint32_t prow = strip_cap_rows(a.max_rows);
+    uint32_t p = cluster_id_();
+    cluster_sync_(); /* every CTA of the cluster runs before shared::cluster reads */
+    uint32_t cur = 0, parity = 0u, pending = 1u, it = 0u, ab = 0u;
+    uint32_t p_prev = 0u;
+    cluster_fill_(a, p, k, cl, tiles, tid, &s_mbar[0]);
+    cp_async_commit_();
+    for (;;) {
+        const uint32_t job = a.props[p].job;
+        const uint32_t R = a.jobs[job].R, B = a.jobs[job].B;
+        const uint32_t ns = (B + 31u) / 32u;
+        const bool ok = R <= a.max_rows && ns <= cl;
+        const bool act = ok && k < ns;
+        const uint32_t c0 = 32u * k;
+        const uint32_t pn = p + ncl;
+        const bool has_next = pn < M;
+        uint32_t* P = P2 + (it & 1u) * prow;
+        float* part = part2 + (it & 1u) * 1024u;
+        cp_async_wait_<0>();
+        if (!mbar_wait_(&s_mbar[cur], (parity >> cur) & 1u)) {
+            atomicOr(a.err, PCS_ERRBIT_TIMEOUT);
+            *s_abort = 1u;
+        }
+        parity ^= 1u << cur;
+        pending &= ~(1u << cur);
+        __syncwarp();
+        uint32_t* T = tiles + cur * tile_words;
+        const Seg sg = seg_(R, w);
+        const uint32_t lc = l >> 2, lo = l & 3u;
+        if (act) {
+            /* phase A1 as in the strip walk, and the strip zeroed */
+            uint32_t run = 0u;
+            for (uint32_t r8 = sg.rb; r8 < sg.re; r8 += 8u) {
+                uint32_t* t = T + (r8 << 5);
+#pragma unroll
+                for (uint32_t j = 0; j < 8u; ++j) {
+                    uint32_t* q = t + (j << 5) + (((lc ^ j) << 2) | lo);
+                    run += *q;
+                    *q = run;
+                }
+            }
+            s_col[w][l] = run;
+            uint32_t z;
+            const TmapDev* map = prop_tmap_(a, p, job, z);
+            if (map) {
+                if (tid == 0u) {
+                    const uint32_t nbox = (R + kBox - 1u) / kBox;
+                    for (uint32_t b = 0; b < nbox; ++b) tma_store_3d_(map, c0, b * kBox, z, zero);
+                    bulk_commit_();
+                }
+            } else if (c0 + l < B) {
+                uint32_t* hist = a.hist + a.props[p].hist_off;
+                for (uint32_t r = sg.rb; r < min(sg.re, R); ++r) __stcs(hist + (uint64_t)r * B + c0 + l, 0u);
+            }
+        }
+        __syncthreads();
+        if (db && has_next && !*s_abort) {
+            cluster_fill_(a, pn, k, cl, tiles + (cur ^ 1u) * tile_words, tid, &s_mbar[cur ^ 1u]);
+            pending |= 1u << (cur ^ 1u);
+            cp_async_commit_();
+        }
+        if (act) {
+            /* phase A2 with row carry 0: the strip's own 2-D prefix sums */
+            uint32_t cc = 0u;
+            for (uint32_t q = 0; q < w; ++q) cc += s_col[q][l];
+            s_K[w][l] = warp_scan_(cc, l);
+            __syncwarp();
+            const uint4* K4 = reinterpret_cast<const uint4*>(s_K[w]);
+            for (uint32_t r = sg.rb + l; r < sg.re; r += 32u) {
+                uint4* row4 = reinterpret_cast<uint4*>(T + (r << 5));
+                const uint32_t m = r & 7u;
+                uint32_t acc = 0u;
+                uint4 o = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                for (uint32_t j = 0; j < 8u; ++j) {
+                    const uint4 v = row4[j ^ m];
+                    const uint4 kk = K4[j];
+                    acc += v.x;
+                    o.x = acc + kk.x;
+                    acc += v.y;
+                    o.y = acc + kk.y;
+                    acc += v.z;
+                    o.z = acc + kk.z;
+                    acc += v.w;
+                    o.w = acc + kk.w;
+                    row4[j ^ m] = o;
+                }
+                P[r] = o.w;
+            }
+        }
+        /* this histogram's last columns, and the previous one's per-lane sums, published */
+        cluster_sync_();
+        for (uint32_t j = 0; j < cl; ++j) ab |= ld_cluster_(s_abort, j);
+        if (ab) break; /* a copy wait ran out somewhere in the cluster (error word set) */
+        if (act) {
+            /* row carry from the strips to the left */
+            for (uint32_t r = tid; r < R; r += kStripThreads) {
+                uint32_t c = 0u;
+                for (uint32_t j = 0; j < k; ++j) c += ld_cluster_(P + r, j);
+                carry[r] = c;
+            }
+            __syncthreads();
+            /* phase B as in the strip walk, the row carry added to each cell */
+            const uint32_t colA = c0 + 2u * w;
+            float a2A = 0.0f, a2B = 0.0f;
+            if (colA < B) {
+                const bool inB = colA + 1u < B;
+                const uint32_t* Tl = T + ((((w >> 1) ^ (l & 7u)) << 2) | ((2u * w) & 3u));
+                const uint32_t* __restrict__ refT = a.jobs[job].ref_sat_t;
+                const uint32_t* refc = refT + (uint64_t)colA * R;
+                const bool exact = T[sw_(R - 1u, 31u)] + carry[R - 1u] < kExactBelow &&
+                                   __ldg(refT + pcs_sat_t_index(R - 1u, B - 1u, R, B)) < kExactBelow;
+                if (exact && inB) {
+                    const uint2* ref2 = reinterpret_cast<const uint2*>(refc);
+#pragma unroll 4
+                    for (uint32_t r = l; r < R; r += 32u) {
+                        const uint2 v = *reinterpret_cast<const uint2*>(Tl + (r << 5));
+                        const uint32_t c = carry[r];
+                        const uint2 o = __ldg(ref2 + r);
+                        const float dA = exact_diff_(v.x + c, o.x);
+                        const float dB = exact_diff_(v.y + c, o.y);
+                        a2A = __fadd_rn(a2A, __fmul_rn(dA, dA));
+                        a2B = __fadd_rn(a2B, __fmul_rn(dB, dB));
+                    }
+                } else if (exact) {
+                    for (uint32_t r = l; r < R; r += 32u) {
+                        const float dA = exact_diff_(Tl[r << 5] + carry[r], __ldg(refc + r));
+                        a2A = __fadd_rn(a2A, __fmul_rn(dA, dA));
+                    }
+                } else {
+                    for (uint32_t r = l; r < R; r += 32u) {
+                        const uint32_t c = carry[r];
+                        if (inB) {
+                            const uint2 v = *reinterpret_cast<const uint2*>(Tl + (r << 5));
+                            const uint2 o = __ldg(reinterpret_cast<const uint2*>(refc) + r);
+                            const float dA = __fsub_rn(__uint2float_rn(v.x + c), __uint2float_rn(o.x));
+                            const float dB = __fsub_rn(__uint2float_rn(v.y + c), __uint2float_rn(o.y));
+                            a2A = __fadd_rn(a2A, __fmul_rn(dA, dA));
+                            a2B = __fadd_rn(a2B, __fmul_rn(dB, dB));
+                        } else {
+                            const float dA = __fsub_rn(__uint2float_rn(Tl[r << 5] + c), __uint2float_rn(__ldg(refc + r)));
+                            a2A = __fadd_rn(a2A, __fmul_rn(dA, dA));
+                        }
+                    }
+                }
+            }
+            part[(2u * w) * 32u + l] = a2A;
+            part[(2u * w + 1u) * 32u + l] = a2B;
+        }
+        /* this tile's generic accesses before its next box fill */
+        fence_proxy_async_();
+        /* CTA 0: the previous histogram, whose sums every CTA published before the barrier */
+        if (k == 0u && it > 0u) cluster_reduce_(a, p_prev, cl, part2 + ((it - 1u) & 1u) * 1024u, s_tot);
+        if (!has_next) break;
+        if (!db) {
+            __syncthreads(); /* the one tile is free */
+            cluster_fill_(a, pn, k, cl, tiles, tid, &s_mbar[0]);
+            pending |= 1u;
+            cp_async_commit_();
+        } else {
+            cur ^= 1u;
+        }
+        p_prev = p;
+        p = pn;
+        ++it;
+    }
+    cluster_sync_(); /* the last histogram's per-lane sums published */
+    if (!ab && k == 0u) cluster_reduce_(a, p, cl, part2 + (it & 1u) * 1024u, s_tot);
+    cluster_sync_(); /* no CTA leaves while CTA 0 reads its sums */
+    cp_async_wait_<0>();
+    for (uint32_t b = 0; b < 2u; ++b)
+        if ((pending >> b) & 1u) mbar_wait_(&s_mbar[b], (parity >> b) & 1u);
+    bulk_wait_all_();
+}
+
+/* Cluster mode (float distance only), clusters of cl CTAs. */
+__global__ void __launch_bounds__(512, 2) k_distance_cluster(DistArgs a, uint32_t db, uint32_t cl)
+{
+    extern __shared__ __align__(16) uint32_t s_mem[];
+    const uint32_t M = *a.n_props;
+    if (cluster_id_() >= M) return; /* whole clusters return */
+    const uint32_t prow = strip_cap_rows(a.max_rows), tile_words = prow * 32u;
+    /* [1 + db][cap rows][32] tiles (1024-byte aligned), a zero box, the row
+     * carries, two last-column arrays, two 32 x 32 per-lane sum arrays */
+    uint32_t* tiles = s_mem + ((1024u - (smem_u32_(s_mem) & 1023u)) & 1023u) / 4u;
+    uint32_t* zero = tiles + (1u + db) * tile_words;
+    uint32_t* carry = zero + kBox * kBox;
+    uint32_t* P2 = carry + prow;
+    float* part2 = reinterpret_cast<float*>(P2 + 2u * prow);
+    __shared__ float s_tot[32];
+    __shared__ uint32_t s_col[16][32];
+    __shared__ __align__(16) uint32_t s_K[16][32];
+    __shared__ __align__(8) uint64_t s_mbar[2];
+    __shared__ uint32_t s_abort;
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init_(&s_mbar[0], kStripThreads);
+        mbar_init_(&s_mbar[1], kStripThreads);
+        mbar_init_fence_();
+        s_abort = 0u;
+    }
+    for (uint32_t i = tid; i < kBox * kBox; i += kStripThreads) zero[i] = 0u;
+    fence_proxy_async_(); /* the zero box, before box stores read it */
+    __syncthreads();
+    strip_cluster_(a, db, cl, M, tiles, tile_words, zero, carry, P2, part2, s_tot, s_col, s_K, s_mbar, &s_abort);
 }
 
 template <bool F64, bool SSD>
@@ -707,29 +1023,40 @@ __global__ void __launch_bounds__(512, 2) k_distance_strip(DistArgs a, uint32_t 
 
 static const size_t kStripSmemMax = 220u * 1024u;
 
-/* 1024 bytes to align the tiles, one or two tiles, the zero box, the row carries */
-static size_t strip_smem_bytes(uint32_t max_rows, bool db)
+/* 1024 bytes to align the tiles, one or two tiles, the zero box, the row
+ * carries; for cluster launches two of each strip's last column and of its
+ * 32 x 32 per-lane sums */
+static size_t strip_smem_bytes(uint32_t max_rows, bool db, uint32_t cl)
 {
     const size_t rows = strip_cap_rows(max_rows);
-    return 1024u + (db ? 2u : 1u) * rows * 32u * sizeof(uint32_t) + kBoxBytes + rows * sizeof(uint32_t);
+    size_t n = 1024u + (db ? 2u : 1u) * rows * 32u * sizeof(uint32_t) + kBoxBytes + rows * sizeof(uint32_t);
+    if (cl > 1u) n += 2u * (rows * sizeof(uint32_t) + 32u * 32u * sizeof(float));
+    return n;
 }
 
-static bool use_strip(uint32_t max_rows) { return strip_smem_bytes(max_rows, false) <= kStripSmemMax; }
-static bool strip_db(uint32_t max_rows) { return strip_smem_bytes(max_rows, true) <= kStripSmemMax; }
+static bool use_strip(uint32_t max_rows, uint32_t cl) { return strip_smem_bytes(max_rows, false, cl) <= kStripSmemMax; }
+static bool strip_db(uint32_t max_rows, uint32_t cl) { return strip_smem_bytes(max_rows, true, cl) <= kStripSmemMax; }
 
-size_t distance_smem_bytes(uint32_t max_rows)
+uint32_t distance_cluster_size(uint32_t max_rows, uint32_t max_bins)
 {
-    if (use_strip(max_rows)) return strip_smem_bytes(max_rows, strip_db(max_rows));
+    const uint32_t strips = (max_bins + 31u) / 32u;
+    if (strips < 2u || strips > kMaxDistCluster) return 0u;
+    return use_strip(max_rows, strips) ? strips : 0u;
+}
+
+size_t distance_smem_bytes(uint32_t max_rows, uint32_t cl)
+{
+    if (use_strip(max_rows, cl)) return strip_smem_bytes(max_rows, strip_db(max_rows, cl), cl);
     return ((size_t)max_rows + (size_t)kDistRowBlock * kPad) * sizeof(uint32_t);
 }
 
-uint32_t distance_block_threads(uint32_t max_rows) { return use_strip(max_rows) ? kStripThreads : 1024u; }
+uint32_t distance_block_threads(uint32_t max_rows) { return use_strip(max_rows, 0u) ? kStripThreads : 1024u; }
 
-int distance_ctas_per_sm(uint32_t max_rows)
+int distance_ctas_per_sm(uint32_t max_rows, uint32_t cl)
 {
-    const size_t smem = distance_smem_bytes(max_rows);
+    const size_t smem = distance_smem_bytes(max_rows, cl);
     int n = 0;
-    if (use_strip(max_rows)) {
+    if (use_strip(max_rows, cl)) {
         cudaFuncSetAttribute(k_distance_strip<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_distance_strip<false, false>, (int)kStripThreads, smem);
     } else {
@@ -739,16 +1066,45 @@ int distance_ctas_per_sm(uint32_t max_rows)
     return n > 0 ? n : 1;
 }
 
-cudaError_t launch_distance(const DistArgs& a, uint32_t grid, cudaStream_t st)
+cudaError_t launch_distance(const DistArgs& a, uint32_t grid, cudaStream_t st, uint32_t cl)
 {
-    const size_t smem = distance_smem_bytes(a.max_rows);
-    if (use_strip(a.max_rows)) {
+    if (cl > 1u && (a.dist_f64 || a.ssd || a.cum_out || !use_strip(a.max_rows, cl) || cl > kMaxDistCluster)) cl = 0u;
+    if (cl > 1u) {
+        /* clusters of cl CTAs where the histograms are tall, or where every
+         * histogram of the launch has a cluster to itself; as many clusters
+         * as fit at once, at most one per histogram slot */
+        const size_t smem = distance_smem_bytes(a.max_rows, cl);
+        cudaError_t e = cudaFuncSetAttribute(k_distance_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cl;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.blockDim = dim3(kStripThreads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cfg.gridDim = dim3(cl);
+        int fit = 0;
+        e = cudaOccupancyMaxActiveClusters(&fit, (void*)k_distance_cluster, &cfg);
+        if (e != cudaSuccess) return e;
+        if (fit > 0 && (strip_cap_rows(a.max_rows) >= kClusterRowsMin || grid <= (uint32_t)fit)) {
+            cfg.gridDim = dim3(std::min<uint32_t>(grid, (uint32_t)fit) * cl);
+            return cudaLaunchKernelEx(&cfg, k_distance_cluster, a, strip_db(a.max_rows, cl) ? 1u : 0u, cl);
+        }
+        cl = 0u;
+    }
+    const size_t smem = distance_smem_bytes(a.max_rows, 0u);
+    if (use_strip(a.max_rows, 0u)) {
         void (*k)(DistArgs, uint32_t);
         if (a.dist_f64) k = a.ssd ? k_distance_strip<true, true> : k_distance_strip<true, false>;
         else k = a.ssd ? k_distance_strip<false, true> : k_distance_strip<false, false>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k<<<grid, kStripThreads, smem, st>>>(a, strip_db(a.max_rows) ? 1u : 0u);
+        k<<<grid, kStripThreads, smem, st>>>(a, strip_db(a.max_rows, 0u) ? 1u : 0u);
         return cudaGetLastError();
     }
     if (a.dist_f64) {

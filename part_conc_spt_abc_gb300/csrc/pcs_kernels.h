@@ -70,16 +70,26 @@ struct DistArgs {
     uint32_t max_rows;          /* rows of the carry array in shared memory */
     const TmapDev* tmaps;       /* nullable: per job (index of jobs), tensor maps over hist */
 };
-cudaError_t launch_distance(const DistArgs& a, uint32_t grid, cudaStream_t st);
+/* grid: CTAs at most (one histogram each).  cl > 1 (at least every job's
+ * strips of 32 bins; 0 or 1: none) allows clusters of cl CTAs, one strip of
+ * a histogram per CTA, which the launch takes where the histograms have at
+ * least kClusterRowsMin rows or `grid` clusters fit at once; otherwise one
+ * CTA walks each histogram's strips.  Variants with the double or integer
+ * sums or the prefix-sum output take no clusters. */
+cudaError_t launch_distance(const DistArgs& a, uint32_t grid, cudaStream_t st, uint32_t cl = 0u);
+/* the cluster size for histograms of up to max_rows x max_bins, or 0 */
+uint32_t distance_cluster_size(uint32_t max_rows, uint32_t max_bins);
+const uint32_t kMaxDistCluster = 8u;
+const uint32_t kClusterRowsMin = 512u;
 /* Host: the tensor map of `depth` histograms of R x B u32 cells stored one
  * after another from `base` (boxes of 32 columns x 32 rows, 128-byte
  * swizzle).  False where the shape does not suit one (B a multiple of 4, R
  * and B at least 32) or the driver refuses it; the kernel then copies cell
  * by cell. */
 bool encode_hist_tmap(TmapDev* out, const uint32_t* base, uint32_t R, uint32_t B, uint64_t depth);
-size_t distance_smem_bytes(uint32_t max_rows);
+size_t distance_smem_bytes(uint32_t max_rows, uint32_t cl = 0u);
 uint32_t distance_block_threads(uint32_t max_rows);
-int distance_ctas_per_sm(uint32_t max_rows);
+int distance_ctas_per_sm(uint32_t max_rows, uint32_t cl = 0u);
 const uint32_t kDistRowBlock = 256;
 
 /* ---------------- ABC-PMC step (kernels_pmc.cu) ---------------- */

@@ -174,7 +174,9 @@ void run_plain(Job& j, uint32_t max_steps, uint32_t queues)
         d.dist_f32 = q.d_dist.as<float>();
         d.err = c.err.as<uint32_t>();
         d.max_rows = j.R;
-        PCS_CUDA(launch_distance(d, 1, q.st));
+        /* the reference's geometry: one CTA per histogram; the persistent
+         * form spreads the histogram's strips over a cluster */
+        PCS_CUDA(launch_distance(d, 1, q.st, ref_geometry ? 0u : distance_cluster_size(j.R, j.B)));
         PCS_CUDA(cudaMemcpyAsync(q.h_dist, q.d_dist.p, sizeof(float), cudaMemcpyDeviceToHost, q.st));
         PCS_CUDA(cudaEventRecord(q.done, q.st));
         q.slot = (int)slot;

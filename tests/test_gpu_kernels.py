@@ -105,6 +105,27 @@ def test_distance_batch_and_sizes(pcs, ctx, oracle, want_f64, want_ssd):
                 assert r["dist_f64"][q] == oracle.distance_kdist_f64(hist[q], ref), (R, B, q)
 
 
+@pytest.mark.parametrize("R,B", [(61, 48), (301, 128), (120, 130), (257, 33), (45, 256), (200, 100), (1001, 256),
+                                 (640, 70)])
+def test_distance_cluster_and_strip_modes(pcs, ctx, oracle, R, B):
+    """Launches whose histograms each get a cluster, and launches of tall
+    histograms (512 rows or more), spread each histogram's strips of 32 bins
+    over a thread-block cluster (one strip per CTA, row carries and per-lane
+    sums exchanged through distributed shared memory; tall histograms
+    outnumbering the clusters are taken in turn); other launches walk the
+    strips in one CTA.  Every histogram gets the oracle's float distance bit
+    for bit either way: two to eight strips, ragged last strips, with tensor
+    maps and cell-by-cell copies (B % 4 != 0)."""
+    rng = np.random.default_rng(R * 1000 + B)
+    ref = np.cumsum(np.cumsum(rng.poisson(0.7, (R, B)), 0), 1).astype(np.uint32)
+    n = 340  # at least the CTAs of one launch (<= 2 per SM): the strip walk
+    hist = rng.poisson(0.7, (n, R, B)).astype(np.uint32)
+    want = np.array([np.float32(oracle.distance_kdist(hist[q], ref)[0]) for q in range(n)])
+    for count in (3, 150, n):
+        got = pcs.scan_distance(ctx, hist[:count], ref)["dist_f32"]
+        assert got.tobytes() == want[:count].tobytes(), (R, B, count)
+
+
 @pytest.mark.parametrize("want_f64,want_ssd", [(False, False), (True, True)])
 def test_distance_large_counts(pcs, ctx, oracle, want_f64, want_ssd):
     """Cumulative counts at and beyond 2^22 (where the strip kernel leaves
