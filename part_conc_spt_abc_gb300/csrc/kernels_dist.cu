@@ -14,6 +14,10 @@
  *            logical warps 2w, 2w+1 while lane l accumulates
  *            (float(cum) - float(ref))^2 for rows l, l+32, ..., the observed
  *            cumulative histogram read from its column-major copy (coalesced);
+ *   k_distance_cluster (histograms of up to 256 bins, where they are tall
+ *            or each has a cluster): a thread-block cluster per histogram,
+ *            one strip per CTA, the row carries and per-lane sums
+ *            exchanged through distributed shared memory;
  *   k_distance (taller histograms, 1024 threads): the same in blocks of
  *            256 rows (tile row pitch 33 words), with the column carry in a
  *            register.
