@@ -445,6 +445,29 @@ def run_plain_config(args, P, ctx, inp, workload, rank):
     ctx.close()
 
 
+def distance_case(args, local):
+    """pcs_scan_distance on COUNT Poisson(0.7) histograms of ROWS x BINS
+    against a cumulative Poisson(0.7) observed histogram: W untimed and K
+    timed calls, wall clock per call including the host-device copies (the
+    kernel's own time comes from the ncu capture this case exists for)."""
+    import part_conc_spt_abc_gb300 as P
+    R, B, n = args.distance_case
+    rng = np.random.default_rng(5)
+    hist = rng.poisson(0.7, (n, R, B)).astype(np.uint32)
+    ref = np.cumsum(np.cumsum(rng.poisson(0.7, (R, B)), 0), 1).astype(np.uint32)
+    ctx = P.Context(local)
+    for _ in range(args.warmup):
+        P.scan_distance(ctx, hist, ref)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        P.scan_distance(ctx, hist, ref)
+    dt = (time.perf_counter() - t0) / max(1, args.steps)
+    ctx.close()
+    return {"metric": "pcs_scan_distance wall time per call (host copies included)", "value": dt * 1e3,
+            "unit": "ms", "higher_is_better": False, "steps": args.steps, "warmup": args.warmup,
+            "config": {"workload": f"{n} histograms of {R} x {B}", "cells": n * R * B}}
+
+
 def config_input(P, ctx, cfg, args):
     """(input, workload text, step text) of configuration cfg on ctx, with the
     context tuned for it (walk, autotuner, round capacity)."""
@@ -652,6 +675,9 @@ def main():
                     help="only the PMC step's time per generation at population 4096, as its own line")
     ap.add_argument("--headline-only", action="store_true",
                     help="configuration 1 alone: no configuration 2 / 3 slices, PMC timing or serving stream")
+    ap.add_argument("--distance-case", type=int, nargs=3, metavar=("ROWS", "BINS", "COUNT"),
+                    help="the distance kernel alone through pcs_scan_distance on COUNT seeded histograms of "
+                         "ROWS x BINS (the small case its ncu captures run on)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -661,6 +687,10 @@ def main():
         return
     if args.serve:
         run_serve(args, local, world)
+        return
+    if args.distance_case:
+        if rank == 0:
+            print(json.dumps(distance_case(args, local)), flush=True)
         return
     if args.pmc_pop4096:
         import part_conc_spt_abc_gb300 as P
