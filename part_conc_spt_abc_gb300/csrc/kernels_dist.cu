@@ -698,17 +698,16 @@ __device__ __forceinline__ void strip_cluster_(const DistArgs& a, uint32_t db, u
         }
         /* this tile's generic accesses before its next box fill */
         fence_proxy_async_();
-        /* CTA 0: the previous histogram, whose sums every CTA published before the barrier */
-        if (k == 0u && it > 0u) cluster_reduce_(a, p_prev, cl, part2 + ((it - 1u) & 1u) * 1024u, s_tot);
-        if (!has_next) break;
-        if (!db) {
-            __syncthreads(); /* the one tile is free */
+        if (!db && has_next) {
+            __syncthreads(); /* the one tile is free: refill it before CTA 0's reduction */
             cluster_fill_(a, pn, k, cl, tiles, tid, &s_mbar[0]);
             pending |= 1u;
             cp_async_commit_();
-        } else {
-            cur ^= 1u;
         }
+        /* CTA 0: the previous histogram, whose sums every CTA published before the barrier */
+        if (k == 0u && it > 0u) cluster_reduce_(a, p_prev, cl, part2 + ((it - 1u) & 1u) * 1024u, s_tot);
+        if (!has_next) break;
+        if (db) cur ^= 1u;
         p_prev = p;
         p = pn;
         ++it;
