@@ -721,7 +721,7 @@ def main():
             line[f"config{extra}"]["step"] = x["run"]["step"]
             line[f"config{extra}"]["tuning"] = x["run"]["tuning"]
         line["pmc_pop4096"] = pmc_at_pop4096(P, local)
-        # the serving stream and the served / plain comparison (spec target)
+        # the serving stream and the served / plain comparison (the batching target)
         line["serve"] = serve_section(args, P, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline and cfg == 1:
         threads = os.cpu_count() or 1

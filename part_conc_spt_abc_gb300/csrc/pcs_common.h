@@ -126,7 +126,7 @@ PCS_HD pcs_u4 pcs_draw(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint3
 struct pcs_philox_pre {
     uint32_t p0;     /* round-1 word 0 without the block */
     uint32_t a3;     /* round-1 word 3 */
-    uint32_t b1;     /* round-2 word 1 */
+    uint32_t b1;     /* word 1 after Philox round 2 */
     uint32_t h3, l3; /* round-3 product of word 0 */
 };
 
@@ -153,7 +153,7 @@ PCS_HD pcs_philox_pre pcs_philox_prepare(uint32_t c0, uint32_t c2, uint32_t c3, 
 PCS_HD pcs_u4 pcs_draw_pre(const pcs_philox_pre& s, uint32_t c1)
 {
     uint32_t h, l;
-    /* round 2: only the product of word 0 depends on the block */
+    /* Philox round 2: only the product of word 0 depends on the block */
     pcs_mulhilo(0xD2511F53u, s.p0 ^ c1, &h, &l);
     const uint32_t b2 = h ^ s.a3 ^ (PCS_PHILOX_K1 + PCS_PHILOX_W1), b3 = l;
     /* round 3: the product of word 0 is fixed */

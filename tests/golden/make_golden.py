@@ -153,7 +153,11 @@ def xml_cases():
             # there is nothing to record (the library reports an XML error)
             res[name] = {"data": os.path.basename(data), "ref": {"crash": True}}
             continue
-        res[name] = {"data": os.path.basename(data), "ref": ref_input_load(inp, data)}
+        ref = ref_input_load(inp, data)
+        if "error" in ref:
+            # the message names the files: record them relative to the repository
+            ref["error"] = ref["error"].replace(xdir + os.sep, "tests/golden/xml/")
+        res[name] = {"data": os.path.basename(data), "ref": ref}
     # the reference's own fixture (test_files/), when the tree is present
     ref_root = O.reference_root()
     tf = os.path.join(ref_root, "test_files") if ref_root else ""
