@@ -88,22 +88,30 @@ __device__ __forceinline__ float cos_ftz_(float x)
     return y;
 }
 
+const float kSqrt2Ln2 = 1.1774100225154747f; /* sqrt(2 ln 2): sqrt(-2 ln u) = sqrt(2 ln 2) sqrt(-log2 u) */
+
 /* Box-Muller on two 32-bit words: u1 in (0,1], angle uniform on [-pi, pi);
- * both normals times `scale` (the walk passes its particle's step sd, so
- * its steps take the normals as they are: one multiply per pair instead of
- * one per coordinate). */
-__device__ __forceinline__ void box_muller_(uint32_t ra, uint32_t rb, float& n0, float& n1, float scale = 1.0f)
+ * both normals times scale = rscale / sqrt(2 ln 2).  The radius is
+ * rscale sqrt(-log2 u): a caller that scales every pair by the same factor
+ * (the walk: its particle's step sd, so its steps take the normals as they
+ * are) folds sqrt(2 ln 2) into it once, one multiply per pair fewer. */
+__device__ __forceinline__ void box_muller_r_(uint32_t ra, uint32_t rb, float& n0, float& n1, float rscale)
 {
     float u = __fmaf_rn(__uint2float_rn(ra), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
-    float x = -1.3862943611198906f * lg2_ftz_(u); /* -2 ln u */
-    float rad = scale * sqrt_ftz_(x);
+    float rad = rscale * sqrt_ftz_(-lg2_ftz_(u));
     float t = __fmaf_rn(__uint2float_rn(rb), 1.4629180792671596e-09f, -3.14159265358979f);
     n0 = rad * sin_ftz_(t);
     n1 = rad * cos_ftz_(t);
 }
 
+/* unit normals */
+__device__ __forceinline__ void box_muller_(uint32_t ra, uint32_t rb, float& n0, float& n1)
+{
+    box_muller_r_(ra, rb, n0, n1, kSqrt2Ln2);
+}
+
 struct Walker {
-    float x, y, z, de, sd, haz;
+    float x, y, z, de, sd, haz; /* sd: the step sd, or (fresh-draw walk) sd x sqrt(2 ln 2) for box_muller_r_ */
     uint32_t k, F, n;  /* n: particle index within the proposal */
     pcs_philox_pre ph; /* the particle's stream with its fixed counter words folded in */
 };
@@ -250,8 +258,9 @@ __device__ __forceinline__ void load_item_(const SimArgs& a, uint32_t item, Prop
 }
 
 /* Initial state of particle n (make_particle, utility.inl:60-99, and the
- * particle's step sd): position, component, half depth, step sd, K. */
-template <bool REPLAY>
+ * particle's step sd): position, component, half depth, step sd, K.
+ * BM_SD: q.sd carries sd x sqrt(2 ln 2), the scale box_muller_r_ takes. */
+template <bool REPLAY, bool BM_SD = false>
 __device__ __forceinline__ void init_walker_(const SimArgs& a, const ItemCtx& c, const JobDev& s_job,
                                              const PropDev& s_prop, const uint32_t* prefix, uint32_t n,
                                              uint32_t slot, uint32_t gt, uint32_t k0, uint32_t k1, Walker& q)
@@ -296,13 +305,15 @@ __device__ __forceinline__ void init_walker_(const SimArgs& a, const ItemCtx& c,
     } else {
         q.sd = s_prop.sd_scale[comp];
     }
+    if (BM_SD) q.sd = __fmul_rn(q.sd, kSqrt2Ln2);
     const bool det = fabsf(q.z) <= q.haz && fabsf(q.x) <= c.hax && fabsf(q.y) <= c.hay;
     q.k = det ? 1u : 0u;
 }
 
 /* The 12 normals of the group of frames s0 .. s0+3: Philox blocks
- * 2+3g .. 4+3g through Box-Muller, times the particle's step sd; or the
- * replayed unit normals (zeros past F). */
+ * 2+3g .. 4+3g through Box-Muller, times the particle's step sd (q.sd holds
+ * sd x sqrt(2 ln 2) on this path); or the replayed unit normals (zeros past
+ * F). */
 template <bool REPLAY>
 __device__ __forceinline__ void group_normals_(const SimArgs& a, const Walker& q, uint32_t s0, float* nn)
 {
@@ -316,8 +327,8 @@ __device__ __forceinline__ void group_normals_(const SimArgs& a, const Walker& q
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
             pcs_u4 r = pcs_draw_pre(q.ph, pcs_ctr_tag(PCS_STREAM_PARTICLE, 2u + 3u * g + (uint32_t)b));
-            box_muller_(r.x, r.y, nn[4 * b + 0], nn[4 * b + 1], q.sd);
-            box_muller_(r.z, r.w, nn[4 * b + 2], nn[4 * b + 3], q.sd);
+            box_muller_r_(r.x, r.y, nn[4 * b + 0], nn[4 * b + 1], q.sd);
+            box_muller_r_(r.z, r.w, nn[4 * b + 2], nn[4 * b + 3], q.sd);
         }
     }
 }
@@ -378,7 +389,7 @@ __device__ __noinline__ void simulate_warp_slices_(const SimArgs& a)
             q.x = q.y = q.z = 0.0f;
             q.sd = 0.0f;
             q.haz = 0.0f;
-            init_walker_<false>(a, c, job, prop, a.counts + prop.counts_off + job.V, n, prop.slot,
+            init_walker_<false, true>(a, c, job, prop, a.counts + prop.counts_off + job.V, n, prop.slot,
                                 pcs_ctr_gen_trial(prop.gen, prop.trial), job.seed_lo, job.seed_hi, q);
             walk_single_<false, AGG>(a, c, nullptr, q);
             if (q.F > 0u && q.k >= c.kmin) record_<AGG>(c, nullptr, q.k, q.de);
@@ -442,7 +453,7 @@ __global__ void __launch_bounds__(sim_max_block(PPT)) k_simulate(SimArgs a)
                 q.sd = 0.0f;
                 q.haz = 0.0f;
                 if (n < a1) {
-                    init_walker_<REPLAY>(a, c, s_job, s_prop, prefix, n, slot, gt, k0, k1, q);
+                    init_walker_<REPLAY, !REPLAY>(a, c, s_job, s_prop, prefix, n, slot, gt, k0, k1, q);
                     fmax = max(fmax, q.F);
                 }
             }
