@@ -481,8 +481,8 @@ __device__ __forceinline__ float exact_diff_(uint32_t s, uint32_t o)
 
 /* Cluster mode (k_distance_cluster), for launches where walking each
  * histogram's strips one after another in one CTA leaves SMs idle or takes
- * long: few histograms, or tall ones.  A cluster
- * of `cl` CTAs takes one histogram at a time, CTA k its strip k (columns
+ * long: few histograms, or tall ones.  A cluster of `cl` CTAs takes one
+ * histogram at a time, CTA k its strip k (columns
  * 32k..32k+31; cl is at least the strips of every job).  Each CTA builds
  * its strip's 2-D prefix sums as if the strip stood alone (row carry 0) and
  * publishes the last column, P_k(r) = the cells of rows <= r in the strip;
@@ -496,7 +496,8 @@ __device__ __forceinline__ float exact_diff_(uint32_t s, uint32_t o)
  * for bit.  One barrier per histogram: P and the per-lane sums alternate
  * between two buffers, and CTA 0 reduces histogram i while the cluster
  * computes histogram i + 1.  The next histogram's strip is copied in while
- * the current one is computed (two tiles).  A copy wait that runs out ends
+ * the current one is computed (two tiles), or, with one tile (tall
+ * histograms), as soon as phase B has read it.  A copy wait that runs out ends
  * the loop on every CTA of the cluster together (each reads all CTAs' flags
  * after the barrier), so no CTA is left waiting at a cluster barrier. */
 __device__ __forceinline__ void cluster_fill_(const DistArgs& a, uint32_t p, uint32_t k, uint32_t cl, uint32_t* T,
