@@ -31,6 +31,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "pcs_common.h"
 #include "pcs_kernels.h"
@@ -1070,6 +1073,32 @@ int distance_ctas_per_sm(uint32_t max_rows, uint32_t cl)
     return n > 0 ? n : 1;
 }
 
+/* Clusters of cl CTAs of k_distance_cluster that fit at once with `smem`
+ * bytes of shared memory each, on the current device; queried once per
+ * (device, cl, smem), since the plain form launches per proposal. */
+static cudaError_t cluster_fit_(cudaLaunchConfig_t& cfg, uint32_t cl, size_t smem, int& fit)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<int, uint32_t, size_t>, int> cache;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const auto key = std::make_tuple(dev, cl, smem);
+    {
+        std::lock_guard<std::mutex> g(mu);
+        const auto it = cache.find(key);
+        if (it != cache.end()) {
+            fit = it->second;
+            return cudaSuccess;
+        }
+    }
+    e = cudaOccupancyMaxActiveClusters(&fit, (void*)k_distance_cluster, &cfg);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(mu);
+    cache[key] = fit;
+    return cudaSuccess;
+}
+
 cudaError_t launch_distance(const DistArgs& a, uint32_t grid, cudaStream_t st, uint32_t cl)
 {
     if (cl > 1u && (a.dist_f64 || a.ssd || a.cum_out || !use_strip(a.max_rows, cl) || cl > kMaxDistCluster)) cl = 0u;
@@ -1093,7 +1122,7 @@ cudaError_t launch_distance(const DistArgs& a, uint32_t grid, cudaStream_t st, u
         cfg.numAttrs = 1;
         cfg.gridDim = dim3(cl);
         int fit = 0;
-        e = cudaOccupancyMaxActiveClusters(&fit, (void*)k_distance_cluster, &cfg);
+        e = cluster_fit_(cfg, cl, smem, fit);
         if (e != cudaSuccess) return e;
         if (fit > 0 && (strip_cap_rows(a.max_rows) >= kClusterRowsMin || grid <= (uint32_t)fit)) {
             cfg.gridDim = dim3(std::min<uint32_t>(grid, (uint32_t)fit) * cl);
